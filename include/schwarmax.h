@@ -1,0 +1,242 @@
+/*
+ * schwarmax.h -- C ABI of the GB300 (sm_103a) SchwarMAX model-evaluation path.
+ *
+ * The reference (Hanyuan0908/SchwarMax) is pure Python + JAX; its hot path is
+ * a chain of jitted functions.  Each entry point below replaces one stage of
+ * that chain (the reference function it stands in for is cited on each), so
+ * that a host holding device buffers (PyTorch tensors here, or any caller via
+ * ctypes/cffi) can run a model evaluation without XLA.
+ *
+ * Conventions
+ *   - Every buffer is a DEVICE pointer owned by the caller, with explicit sizes.
+ *     Arrays named "SoA (k, n)" hold component c of item i at [c*n + i].
+ *   - `precision` selects the element type of the floating-point buffers of a
+ *     call: SMX_FP32 -> float, SMX_FP64 -> double.  Parameter structs are
+ *     always double.
+ *   - `stream` is a cudaStream_t (NULL = legacy default stream).  Calls are
+ *     asynchronous with respect to the host unless documented otherwise.
+ *   - Every call returns an smx_status; no exception crosses the ABI.  The
+ *     message of the last failure on the calling thread is returned by
+ *     smx_last_error().
+ *   - Units: kpc, Gyr, Msun; velocities in kpc/Gyr unless stated; angles in
+ *     radians; G = 4.498502151469554e-6 kpc^3 / Msun / Gyr^2.
+ */
+#ifndef SCHWARMAX_H
+#define SCHWARMAX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    SMX_OK = 0,
+    SMX_ERR_ARGUMENT = 1,      /* bad size, pointer or option */
+    SMX_ERR_UNSUPPORTED = 2,   /* model or option the library does not implement */
+    SMX_ERR_NONFINITE = 3,     /* non-finite input or result where it is not allowed */
+    SMX_ERR_ITERATION_CAP = 4, /* an iteration limit was reached */
+    SMX_ERR_CUDA = 5,          /* CUDA runtime / library error */
+    SMX_ERR_WORKSPACE = 6,     /* workspace too small */
+    SMX_ERR_NUMERIC = 7        /* factorisation failed (matrix not positive definite) */
+} smx_status;
+
+typedef enum { SMX_FP32 = 0, SMX_FP64 = 1 } smx_precision;
+
+/* Canonical potential Phi = NFW + Miyamoto-Nagai + Dehnen-Aly T (bar) +
+ * Dehnen-Aly V (bulge), all centred at the origin with symmetry axis +z.
+ * Replaces potential_func / density_func of likelihood.py:13-71 (built from
+ * potentials.py:18-65 and dehnen_bar.py:1318-1543).  The bar is a T3 model and
+ * the bulge a V4 model; gamma is the needle slope (dehnen_bar.py:211-241). */
+typedef struct {
+    double halo_M, halo_Rs, halo_qa, halo_qb, halo_qc;      /* NFW: M = 10**logM */
+    double disc_M, disc_a, disc_b;                            /* MN: M, Rs_disc, Hs_disc */
+    double bar_M, bar_a, bar_b, bar_L, bar_gamma;             /* T3 */
+    double bulge_M, bulge_a, bulge_b, bulge_L, bulge_gamma;   /* V4 */
+} smx_potential;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int smx_version(void);
+const char *smx_status_string(int status);
+/* Copies the last error message of the calling thread into buf (NUL
+ * terminated, truncated to len) and returns its full length. */
+size_t smx_last_error(char *buf, size_t len);
+
+/* Phi, -grad Phi and stellar rho at n points.  x, y, z: (n,); any output may
+ * be NULL.  Replaces potential_func, acc_fn (model.py:152-157, jax.grad) and
+ * density_func (likelihood.py:13-71). */
+int smx_potential_eval(const smx_potential *pot, int precision, const void *x, const void *y,
+                       const void *z, int64_t n, void *phi, void *ax, void *ay, void *az,
+                       void *rho, void *stream);
+
+/* Per-particle set-up of the orbit library, fused: axisymmetric Jeans
+ * velocities (jeans.py:8-93, 1000-point trapezoids), V_c and T_orb by central
+ * differences (utils.py:182-273) and the jitter into n_real realisations
+ * (model.py:127-148).
+ *   pos      SoA (3, n)          particle positions (dict_data['w0'])
+ *   normals  SoA (3, n)          standard normals g1, g2, g3
+ *   uniforms (6, n, n_real)      uniform [0,1) draws for the jitter
+ * Outputs (NULL allowed for the optional ones):
+ *   w_out    SoA (6, n*n_real)   start states, orbit index p*n_real + r
+ *   t_total  (n*n_real)          n_periods * T_orb
+ *   dt_init  (n*n_real)          T_orb / steps_per_period
+ *   w0_new   SoA (6, n)  opt.    un-jittered Jeans state
+ *   t_orb    (n)         opt.
+ *   vc       (n)         opt. */
+int smx_initial_conditions(const smx_potential *pot, int precision, const void *pos,
+                           const void *normals, const void *uniforms, int64_t n, int n_real,
+                           double n_periods, double steps_per_period, void *w_out,
+                           void *t_total, void *dt_init, void *w0_new, void *t_orb, void *vc,
+                           void *stream);
+
+/* 3-D density target (model.py:192-213): for each cell c,
+ * out[c] = dR dz dphi mean_j rho(R_j cos phi_j, R_j sin phi_j, z_j) R_j with
+ * (R,z,phi)_j = (R,z,phi)_c + (sample_j - 1/2)(dR,dz,dphi).
+ *   R_grid, z_grid, phi_grid (n_cells) and sample (n_sample, 3) are double;
+ *   out (n_cells) has the call's precision. */
+int smx_density_target(const smx_potential *pot, int precision, const double *R_grid,
+                       const double *z_grid, const double *phi_grid, int64_t n_cells, double dR,
+                       double dz, double dphi, const double *sample, int n_sample, void *out,
+                       void *stream);
+
+/* ---------------------------------------------------------------- orbits */
+enum { SMX_MODE_REFERENCE = 0, SMX_MODE_SAMPLED = 1 };
+
+typedef struct {
+    int mode;              /* SMX_MODE_REFERENCE: n_attempts BS23 attempts per orbit,
+                              each accepted attempt one sample of weight dt
+                              (integrates.py:90-205).
+                              SMX_MODE_SAMPLED: integrate to t_total and emit
+                              n_samples uniform-time samples (cubic Hermite dense
+                              output), weight t_total/n_samples each. */
+    int store_all;         /* reference mode: keep every attempt (rejected ones with
+                              weight 0) in slot = attempt index, as the trajectory
+                              variant does (integrates.py:319-512) */
+    int n_attempts;        /* reference mode: N_max */
+    int n_samples;         /* sampled mode */
+    int64_t max_attempts;  /* sampled mode: cap per orbit (status bit 2 when hit) */
+    double atol, rtol, dt_min, dt_max;
+    double omega;          /* frame angular velocity Omega = -Omega_bar (kpc/Gyr) */
+} smx_integrator;
+
+/* Per-orbit record written by smx_integrate (array of n_orb, precision of the
+ * call):  t_final, EJ0, EJ_final, weight_sum, n_accepted, n_attempts. */
+enum { SMX_INFO_T = 0, SMX_INFO_EJ0 = 1, SMX_INFO_EJ = 2, SMX_INFO_WSUM = 3,
+       SMX_INFO_NACC = 4, SMX_INFO_NATT = 5, SMX_INFO_FIELDS = 6 };
+
+/* Adaptive Bogacki-Shampine 3(2) orbits in the bar frame with the canonical
+ * forces inline (integrate_adaptive_barred_chunked, integrates.py:37-238;
+ * _deriv_barred 8-27; _compute_EJ 29-35).  One GPU thread per orbit; a device
+ * work queue hands out orbits.
+ *   w0       SoA (6, n_orb)
+ *   dt_init  (n_orb)
+ *   t_total  (n_orb)           sampled mode: end time; unused otherwise
+ *   samples  (7, n_orb, slots) x, y, z, vx, vy, vz, weight of each stored sample
+ *   n_stored (n_orb) int32     samples written per orbit
+ *   info     (SMX_INFO_FIELDS, n_orb)
+ *   status   (n_orb) int32     bit 0 non-finite state, bit 1 attempt cap,
+ *                              bit 2 slot overflow (0 = clean)
+ *   queue    one int32 of device scratch (the call zeroes it). */
+int smx_integrate(const smx_potential *pot, const smx_integrator *cfg, int precision,
+                  const void *w0, const void *dt_init, const void *t_total, int64_t n_orb,
+                  int64_t slots, void *samples, int32_t *n_stored, void *info, int32_t *status,
+                  int32_t *queue, void *stream);
+
+/* ------------------------------------------------------------- projection */
+typedef struct {
+    int n_part, n_real;
+    int nR, nz, nphi;           /* Rzphi grid, cell = iR + nR*(iz + nz*iphi) */
+    double R_lo, R_hi, z_lo, z_hi, phi_lo, phi_hi;
+    int nX, nY;                 /* sky grid, pixel = ix + nX*iy */
+    double X_lo, X_hi, Y_lo, Y_hi;
+    int n_bins;                 /* Voronoi apertures */
+    int symmetry;               /* 1: fourfold bar images (library), 0: none (trajectory) */
+    double rot[9];              /* row-major X = rot @ x (makeRotationMatrix, utils.py:176-179) */
+} smx_binning;
+
+/* Library row layout (rows = n_cells + 6*n_bins): [Rzphi | xy | h0 | h1 | h2 | h3 | h4]. */
+
+/* Projection, aperture assignment and Gauss-Hermite accumulation of stored
+ * samples, with the T_integrated normalisation, the E_J / time validity rule
+ * and the realisation mean fused (integrates.py:115-174, 207-238, 287-298).
+ * One CTA per particle accumulates its n_real realisations in a
+ * shared-memory histogram.  Cell indices use IEEE single (double) operations
+ * in the order of assign_regular_grid (utils.py:10-42) without contraction.
+ *   samples, n_stored, info: as written by smx_integrate (orbit p*n_real + r)
+ *   t_total     (n_part*n_real)        validity needs t_final > t_total/10
+ *   bin_mapping (nX*nY + 1) int32      last entry is the -1 sentinel
+ *   num_per_bin (n_bins) double; v0, s (n_bins) double (km/s)
+ *   library     (n_part, rows)         precision of the call
+ *   valid       (n_part*n_real) int8   optional */
+int smx_project_bin(const smx_binning *geo, int precision, const void *samples,
+                    const int32_t *n_stored, int64_t slots, const void *info,
+                    const void *t_total, const int32_t *bin_mapping, const double *num_per_bin,
+                    const double *v0, const double *s, void *library, int8_t *valid,
+                    void *stream);
+
+/* ------------------------------------------------------------------- NNLS */
+enum { SMX_NNLS_FP64 = 0, SMX_NNLS_MIXED = 1 };
+
+typedef struct {
+    int64_t n;          /* orbits (columns) */
+    int64_t m;          /* design rows */
+    int64_t n_rhs;      /* bootstrap right-hand sides */
+    int64_t ld_lib;     /* row stride of the library (rows per orbit) */
+    int lib_precision;  /* SMX_FP32 / SMX_FP64 element type of the library */
+    int mode;           /* SMX_NNLS_FP64 or SMX_NNLS_MIXED */
+    int maxiter;
+    double lambda_reg;
+    double w_init;      /* initial w = z (sum(y_Rzphi)/n) */
+} smx_nnls_problem;
+
+/* Bytes of device workspace smx_nnls_admm needs. */
+int smx_nnls_workspace_size(const smx_nnls_problem *prob, size_t *bytes);
+
+/* ADMM NNLS shared by n_rhs right-hand sides (solve_nnls_admm_bootstrap,
+ * nnls.py:68-166; with n_rhs = 1 it is solve_nnls_admm, nnls.py:6-66).
+ * The design matrix is U[r, i] = library[i*ld_lib + row_map[r]] * row_scale[r];
+ * Q = U^T U + (lambda/n) I, rho = tr(Q)/n and each of maxiter iterations
+ * applies (Q + rho I)^-1, evaluated through the Woodbury identity with the
+ * m x m matrix rho' I + U U^T (rho' = rho + lambda/n) factorised by Cholesky.
+ *   row_map (m) int32, row_scale (m) double, Y (n_rhs, m) double scaled data
+ *   Z_out   (n_rhs, n) double: final z of every right-hand side. */
+int smx_nnls_admm(const smx_nnls_problem *prob, const void *library, const int32_t *row_map,
+                  const double *row_scale, const double *Y, double *Z_out, void *workspace,
+                  size_t workspace_bytes, void *stream);
+
+/* ------------------------------------------------------- model maps, chi2 */
+typedef struct {
+    int64_t n;           /* orbits */
+    int64_t n_rhs;       /* weight vectors */
+    int64_t ld_lib;      /* library row stride */
+    int lib_precision;
+    int n_cells, n_bins;
+    double lum_factor;   /* mean_mass_per_orb / (M/L) */
+    double sigma_amplify;
+} smx_maps_problem;
+
+/* Model maps per weight vector and the chi^2 of each
+ * (compute_model_single, model.py:14-68; h_to_V_sigma, ghmoments.py:53-78;
+ * model_likelihood, likelihood.py:192-238).
+ *   W (n_rhs, n) double.  gamma_kin, v0, s (n_bins) double.
+ *   data: y_rz (n_cells) normalised 3-D target, y_xy (n_bins) observed surface
+ *         density, y_xy_boot (n_rhs, n_bins), y_h_boot (4, n_rhs, n_bins),
+ *         sig_h_raw (4, n_bins) = h_k errors + EPSILON, all double.  The chi^2
+ *         uses sigma = 0.1 y_rz, 0.1 y_xy and sig_h_raw, each times sigma_amplify.
+ *   maps_out (n_rhs, n_cells + 7*n_bins) double, layout
+ *         [density_3d | surface | h1 | h2 | h3 | h4 | V | sigma]  (optional)
+ *   logl_out (n_rhs) double: -1/2 chi^2 of each weight vector, with the
+ *         Rzphi term summed over all vectors as the reference does. */
+int smx_model_maps(const smx_maps_problem *prob, const void *library, const double *W,
+                   const double *gamma_kin, const double *v0, const double *s,
+                   const double *y_rz, const double *y_xy, const double *y_xy_boot, const double *y_h_boot,
+                   const double *sig_h_raw, double *maps_out, double *logl_out,
+                   void *workspace, size_t workspace_bytes, void *stream);
+
+int smx_model_maps_workspace_size(const smx_maps_problem *prob, size_t *bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SCHWARMAX_H */

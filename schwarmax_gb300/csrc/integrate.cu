@@ -1,0 +1,227 @@
+// Orbit integrator: adaptive Bogacki-Shampine 3(2) in the bar's rotating frame
+// (integrates.py:8-238 for the stepper, the E_J record and the sampling rule).
+//
+// One thread owns one orbit at a time, with the state, the FSAL derivative and
+// the step size in registers and the canonical forces evaluated inline.  Orbits
+// are handed out by a device counter, so in the sampled mode (uneven step
+// counts) a lane that finishes early takes the next orbit instead of idling.
+// Samples are written orbit-major, (7, n_orb, slots), so the projection kernel
+// reads each orbit contiguously; consecutive writes of one thread land in the
+// same sectors and merge in L2.
+#include "smx_internal.cuh"
+
+namespace smx {
+
+template <typename T> struct IntegT {
+    T atol, rtol, dt_min, dt_max, om;
+    int mode, store_all, n_attempts, n_samples;
+    long long max_attempts;
+};
+
+template <typename T>
+__device__ __forceinline__ void rhs(const PotT<T> &P, T om, const T (&y)[6], T (&f)[6]) {
+    T p, gx, gy, gz;
+    potential<T, false, true>(P, y[0], y[1], y[2], p, gx, gy, gz);
+    f[0] = y[3] + om * y[1];
+    f[1] = y[4] - om * y[0];
+    f[2] = y[5];
+    f[3] = -gx + om * y[4];
+    f[4] = -gy - om * y[3];
+    f[5] = -gz;
+}
+
+template <typename T>
+__device__ __forceinline__ T jacobi(const PotT<T> &P, T om, const T (&y)[6]) {
+    const T ek = T(0.5) * (y[3] * y[3] + y[4] * y[4] + y[5] * y[5]);
+    return ek + phi_only(P, y[0], y[1], y[2]) - om * (y[0] * y[4] - y[1] * y[3]);
+}
+
+template <typename T>
+__device__ __forceinline__ void put(T *samples, int64_t n_orb, int64_t slots, int64_t orb, int64_t slot,
+                                    const T (&y)[6], T w) {
+    T *base = samples + orb * slots + slot;
+    const int64_t cs = n_orb * slots;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) base[c * cs] = y[c];
+    base[6 * cs] = w;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) integrate_kernel(PotT<T> P, IntegT<T> I, const T *__restrict__ w0,
+                                                       const T *__restrict__ dt0, const T *__restrict__ t_end,
+                                                       int64_t n_orb, int64_t slots, T *samples,
+                                                       int32_t *n_stored, T *info, int32_t *status,
+                                                       int32_t *queue) {
+    const T e1 = T(-5.0 / 72.0), e2 = T(1.0 / 12.0), e3 = T(1.0 / 9.0), e4 = T(-1.0 / 8.0);
+    const T b1 = T(2.0 / 9.0), b2 = T(1.0 / 3.0), b3 = T(4.0 / 9.0);
+    const T om = I.om;
+    for (;;) {
+        const int64_t orb = atomicAdd(queue, 1);
+        if (orb >= n_orb) break;
+        T y[6], k1[6], k2[6], k3[6], yn[6], yt[6];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) y[c] = w0[c * n_orb + orb];
+        T dt = dt0[orb];
+        T t = T(0);
+        rhs(P, om, y, k1);
+        const T EJ0 = jacobi(P, om, y);
+        int flags = 0;
+        int64_t n_acc = 0, att = 0, stored = 0;
+        T wsum = T(0);
+        const bool sampled = I.mode == SMX_MODE_SAMPLED;
+        const T Tend = sampled ? t_end[orb] : T(0);
+        const T h = sampled ? Tend / T(I.n_samples) : T(0);
+        int64_t next = 0;
+        const int64_t att_cap = sampled ? I.max_attempts : (int64_t)I.n_attempts;
+        while (att < att_cap && (!sampled || next < I.n_samples)) {
+            ++att;
+#pragma unroll
+            for (int c = 0; c < 6; ++c) yt[c] = y[c] + T(0.5) * dt * k1[c];
+            rhs(P, om, yt, k2);
+#pragma unroll
+            for (int c = 0; c < 6; ++c) yt[c] = y[c] + T(0.75) * dt * k2[c];
+            rhs(P, om, yt, k3);
+#pragma unroll
+            for (int c = 0; c < 6; ++c) yn[c] = y[c] + dt * (b1 * k1[c] + b2 * k2[c] + b3 * k3[c]);
+            T k4[6];
+            rhs(P, om, yn, k4);
+            T s = T(0);
+#pragma unroll
+            for (int c = 0; c < 6; ++c) {
+                const T err = dt * (e1 * k1[c] + e2 * k2[c] + e3 * k3[c] + e4 * k4[c]);
+                const T ay = M<T>::abs(y[c]), ayn = M<T>::abs(yn[c]);
+                const T sc = I.atol + I.rtol * (ay > ayn ? ay : ayn);
+                const T q = err / sc;
+                s += q * q;
+            }
+            const T en = M<T>::sqrt(s / T(6));
+            if (!(en == en)) {   // NaN: the orbit is lost (it fails the E_J test downstream)
+                flags |= 1;
+                break;
+            }
+            const bool accept = en <= T(1);
+            if (accept) {
+                ++n_acc;
+                const T t1 = t + dt;
+                if (sampled) {
+                    // emit all sample times (j + 1/2) h inside (t, t1] by cubic Hermite
+                    while (next < I.n_samples) {
+                        const T tj = (T(next) + T(0.5)) * h;
+                        if (tj > t1) break;
+                        const T th = (tj - t) / dt;
+                        const T th2 = th * th, th3 = th2 * th;
+                        const T h00 = T(2) * th3 - T(3) * th2 + T(1);
+                        const T h10 = (th3 - T(2) * th2 + th) * dt;
+                        const T h01 = T(-2) * th3 + T(3) * th2;
+                        const T h11 = (th3 - th2) * dt;
+                        T ys[6];
+#pragma unroll
+                        for (int c = 0; c < 6; ++c) ys[c] = h00 * y[c] + h10 * k1[c] + h01 * yn[c] + h11 * k4[c];
+                        if (next < slots) put(samples, n_orb, slots, orb, next, ys, h);
+                        else flags |= 4;
+                        wsum += h;
+                        ++next;
+                    }
+                    stored = next < slots ? next : slots;
+                }
+#pragma unroll
+                for (int c = 0; c < 6; ++c) {
+                    y[c] = yn[c];
+                    k1[c] = k4[c];
+                }
+                if (!sampled) {
+                    const int64_t slot = I.store_all ? att - 1 : stored;
+                    if (slot < slots) put(samples, n_orb, slots, orb, slot, y, dt);
+                    else flags |= 4;
+                    stored = slot + 1;
+                    wsum += dt;
+                }
+                t = t1;
+            } else if (!sampled && I.store_all) {
+                const int64_t slot = att - 1;
+                if (slot < slots) put(samples, n_orb, slots, orb, slot, y, T(0));
+                else flags |= 4;
+                stored = slot + 1;
+            }
+            T sf = T(0.9) * M<T>::rcbrt(en > T(1e-10) ? en : T(1e-10));
+            sf = sf < T(0.2) ? T(0.2) : (sf > T(5) ? T(5) : sf);
+            T dn = dt * sf;
+            dt = dn < I.dt_min ? I.dt_min : (dn > I.dt_max ? I.dt_max : dn);
+        }
+        if (sampled && next < I.n_samples) flags |= 2;
+        if (stored > slots) stored = slots;
+        n_stored[orb] = (int32_t)stored;
+        const T EJ = jacobi(P, om, y);
+        info[SMX_INFO_T * n_orb + orb] = t;
+        info[SMX_INFO_EJ0 * n_orb + orb] = EJ0;
+        info[SMX_INFO_EJ * n_orb + orb] = EJ;
+        info[SMX_INFO_WSUM * n_orb + orb] = wsum;
+        info[SMX_INFO_NACC * n_orb + orb] = T(n_acc);
+        info[SMX_INFO_NATT * n_orb + orb] = T(att);
+        status[orb] = flags;
+    }
+}
+
+template <typename T>
+static int launch(const smx_potential *pot, const smx_integrator *cfg, const void *w0, const void *dt_init,
+                  const void *t_total, int64_t n_orb, int64_t slots, void *samples, int32_t *n_stored, void *info,
+                  int32_t *status, int32_t *queue, cudaStream_t s) {
+    IntegT<T> I;
+    I.atol = T(cfg->atol);
+    I.rtol = T(cfg->rtol);
+    I.dt_min = T(cfg->dt_min);
+    I.dt_max = T(cfg->dt_max);
+    I.om = T(cfg->omega);
+    I.mode = cfg->mode;
+    I.store_all = cfg->store_all;
+    I.n_attempts = cfg->n_attempts;
+    I.n_samples = cfg->n_samples;
+    I.max_attempts = cfg->max_attempts;
+    SMX_TRY_CUDA(cudaMemsetAsync(queue, 0, sizeof(int32_t), s));
+    int dev = 0, sms = 0;
+    SMX_TRY_CUDA(cudaGetDevice(&dev));
+    SMX_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    int per_sm = 0;
+    SMX_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, integrate_kernel<T>, 128, 0));
+    if (per_sm < 1) per_sm = 1;
+    int64_t blocks = (n_orb + 127) / 128;
+    const int64_t resident = (int64_t)sms * per_sm;
+    if (blocks > resident) blocks = resident;
+    integrate_kernel<T><<<(unsigned)blocks, 128, 0, s>>>(make_pot<T>(*pot), I, (const T *)w0, (const T *)dt_init,
+                                                         (const T *)t_total, n_orb, slots, (T *)samples, n_stored,
+                                                         (T *)info, status, queue);
+    SMX_TRY_CUDA(cudaGetLastError());
+    return SMX_OK;
+}
+
+}  // namespace smx
+
+using namespace smx;
+
+extern "C" int smx_integrate(const smx_potential *pot, const smx_integrator *cfg, int precision, const void *w0,
+                             const void *dt_init, const void *t_total, int64_t n_orb, int64_t slots, void *samples,
+                             int32_t *n_stored, void *info, int32_t *status, int32_t *queue, void *stream) {
+    int st = validate_potential(pot);
+    if (st) return st;
+    if (!cfg) return set_error(SMX_ERR_ARGUMENT, "smx_integrate: cfg is NULL");
+    if (n_orb < 0 || slots < 1) return set_error(SMX_ERR_ARGUMENT, "smx_integrate: bad sizes");
+    if (n_orb == 0) return SMX_OK;
+    if (!w0 || !dt_init || !samples || !n_stored || !info || !status || !queue)
+        return set_error(SMX_ERR_ARGUMENT, "smx_integrate: NULL buffer");
+    if (cfg->mode == SMX_MODE_REFERENCE) {
+        if (cfg->n_attempts < 1) return set_error(SMX_ERR_ARGUMENT, "n_attempts must be >= 1");
+    } else if (cfg->mode == SMX_MODE_SAMPLED) {
+        if (cfg->n_samples < 1 || cfg->max_attempts < 1 || !t_total)
+            return set_error(SMX_ERR_ARGUMENT, "sampled mode needs n_samples, max_attempts and t_total");
+    } else {
+        return set_error(SMX_ERR_ARGUMENT, "unknown integrator mode %d", cfg->mode);
+    }
+    if (!(cfg->atol > 0) || !(cfg->rtol >= 0) || !(cfg->dt_min > 0) || !(cfg->dt_max >= cfg->dt_min))
+        return set_error(SMX_ERR_ARGUMENT, "bad tolerances or step bounds");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (precision == SMX_FP32)
+        return launch<float>(pot, cfg, w0, dt_init, t_total, n_orb, slots, samples, n_stored, info, status, queue, s);
+    if (precision == SMX_FP64)
+        return launch<double>(pot, cfg, w0, dt_init, t_total, n_orb, slots, samples, n_stored, info, status, queue, s);
+    return set_error(SMX_ERR_ARGUMENT, "bad precision %d", precision);
+}

@@ -1,0 +1,236 @@
+// Projection + binning: stored orbit samples -> one library column per particle.
+//
+// One CTA per particle.  Its n_real realisations are accumulated into a single
+// shared-memory row [Rzphi | xy | h0..h4]; each sample's weight is pre-scaled
+// by valid_r / ((sum_r valid_r + 0.1) * T_r), which folds the per-realisation
+// normalisation, the validity mask and the realisation mean of
+// integrates.py:207-238, 287-298 into the accumulation.  Each thread walks its
+// own contiguous stretch of the orbit, so the 32 lanes of a warp sit at
+// different orbital phases and rarely hit the same histogram cell in the same
+// atomic.  Cell indices follow utils.py:10-42 with explicitly rounded IEEE
+// operations (no FMA contraction), in the order
+//   norm = (p - lo) / (hi - lo); k = floor(norm * n); clip; oob if norm >= 1 or < 0.
+#include "smx_internal.cuh"
+
+namespace smx {
+
+template <typename T> struct RN;
+template <> struct RN<float> {
+    static __device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+    static __device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+    static __device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+    static __device__ __forceinline__ float div(float a, float b) { return __fdiv_rn(a, b); }
+    static __device__ __forceinline__ float sqrt(float a) { return __fsqrt_rn(a); }
+};
+template <> struct RN<double> {
+    static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+    static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+    static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+    static __device__ __forceinline__ double div(double a, double b) { return __ddiv_rn(a, b); }
+    static __device__ __forceinline__ double sqrt(double a) { return __dsqrt_rn(a); }
+};
+
+template <typename T> struct GeoT {
+    T lo[3], span[3], fn[3];   // Rzphi grid
+    int n[3];
+    T xlo[2], xspan[2], xfn[2];  // sky grid
+    int nx[2];
+    T rot[9];
+    int n_cells, n_pix, n_bins, rows, n_part, n_real, symmetry;
+};
+
+// Returns the flat cell of (a, b, c) or `oob` when any normalised coordinate is
+// outside [0, 1).
+template <typename T, int D>
+__device__ __forceinline__ int grid_cell(const T (&v)[D], const T *lo, const T *span, const T *fn, const int *n,
+                                         int oob) {
+    int flat = 0, stride = 1;
+    bool out = false;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+        const T norm = RN<T>::div(RN<T>::sub(v[d], lo[d]), span[d]);
+        out |= !(norm < T(1)) || norm < T(0);
+        int k = (int)floor(RN<T>::mul(norm, fn[d]));
+        k = k < 0 ? 0 : (k > n[d] - 1 ? n[d] - 1 : k);
+        flat += k * stride;
+        stride *= n[d];
+    }
+    return out ? oob : flat;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) project_bin_kernel(GeoT<T> G, const T *__restrict__ samples,
+                                                         const int32_t *__restrict__ n_stored, int64_t slots,
+                                                         const T *__restrict__ info, const T *__restrict__ t_total,
+                                                         const int32_t *__restrict__ bin_mapping,
+                                                         const double *__restrict__ num_per_bin,
+                                                         const double *__restrict__ v0g,
+                                                         const double *__restrict__ sg, double area_pixel,
+                                                         T *library, int8_t *valid_out) {
+    extern __shared__ unsigned char smem_raw[];
+    T *acc = reinterpret_cast<T *>(smem_raw);
+    __shared__ double scale_r[8];
+    const int p = blockIdx.x;
+    const int n_real = G.n_real;
+    const int64_t n_orb = (int64_t)G.n_part * n_real;
+    for (int i = threadIdx.x; i < G.rows; i += blockDim.x) acc[i] = T(0);
+    if (threadIdx.x == 0) {
+        double v[8];
+        double nv = 0;
+        for (int r = 0; r < n_real; ++r) {
+            const int64_t o = (int64_t)p * n_real + r;
+            const double EJ0 = (double)info[SMX_INFO_EJ0 * n_orb + o];
+            const double EJ = (double)info[SMX_INFO_EJ * n_orb + o];
+            const double tf = (double)info[SMX_INFO_T * n_orb + o];
+            // evaluated in the working precision, as |EJ/EJ0 - 1| < 0.1 and t > T/10
+            const T dE = M<T>::abs(T(EJ) / T(EJ0) - T(1));
+            const bool ok = (dE < T(0.1)) && (T(tf) > t_total[o] / T(10));
+            v[r] = ok ? 1.0 : 0.0;
+            nv += v[r];
+            if (valid_out) valid_out[o] = ok ? 1 : 0;
+        }
+        for (int r = 0; r < n_real; ++r) {
+            const int64_t o = (int64_t)p * n_real + r;
+            const double wsum = (double)info[SMX_INFO_WSUM * n_orb + o];
+            const double Ti = (G.symmetry ? 4.0 : 1.0) * wsum + kEps;
+            scale_r[r] = v[r] / ((nv + 0.1) * Ti);
+        }
+    }
+    __syncthreads();
+    const int off_xy = G.n_cells;
+    const int off_h = G.n_cells + G.n_bins;
+    const int nb = G.n_bins;
+    const T kms = T(kKpcGyrToKms);
+    const T isq2pi = T(0.3989422804014327);
+    const T sq2 = T(1.4142135623730951), sq3 = T(1.7320508075688772), isq2 = T(0.7071067811865476),
+            isq3 = T(0.5773502691896258);
+    const int n_img = G.symmetry ? 4 : 1;
+    for (int r = 0; r < n_real; ++r) {
+        const double scd = scale_r[r];
+        if (scd == 0.0) continue;
+        const T sc = T(scd);
+        const int64_t o = (int64_t)p * n_real + r;
+        const int64_t S = n_stored[o];
+        const int64_t lo_j = S * threadIdx.x / blockDim.x;
+        const int64_t hi_j = S * (threadIdx.x + 1) / blockDim.x;
+        const T *base = samples + o * slots;
+        const int64_t cs = n_orb * slots;
+        for (int64_t j = lo_j; j < hi_j; ++j) {
+            const T wraw = base[6 * cs + j];
+            if (wraw == T(0)) continue;   // rejected attempts carry no weight
+            const T w = wraw * sc;
+            const T q[6] = {base[j], base[cs + j], base[2 * cs + j], base[3 * cs + j], base[4 * cs + j], base[5 * cs + j]};
+            for (int im = 0; im < n_img; ++im) {
+                // sign patterns of integrates.py:74-79
+                const T sxy = (im >= 2) ? T(-1) : T(1);
+                const T sz = (im == 1 || im == 3) ? T(-1) : T(1);
+                const T x = sxy * q[0], y = sxy * q[1], z = sz * q[2];
+                const T vx = sxy * q[3], vy = sxy * q[4], vz = sz * q[5];
+                const T R = RN<T>::sqrt(RN<T>::add(RN<T>::mul(x, x), RN<T>::mul(y, y)));
+                const T ph = M<T>::atan2(y, x);
+                const T cyl[3] = {R, z, ph};
+                const int cell = grid_cell<T, 3>(cyl, G.lo, G.span, G.fn, G.n, G.n_cells);
+                if (cell < G.n_cells) atomicAdd(&acc[cell], w);
+                const T X = RN<T>::add(RN<T>::add(RN<T>::mul(G.rot[0], x), RN<T>::mul(G.rot[1], y)), RN<T>::mul(G.rot[2], z));
+                const T Y = RN<T>::add(RN<T>::add(RN<T>::mul(G.rot[3], x), RN<T>::mul(G.rot[4], y)), RN<T>::mul(G.rot[5], z));
+                const T sky[2] = {X, Y};
+                const int pix = grid_cell<T, 2>(sky, G.xlo, G.xspan, G.xfn, G.nx, G.n_pix);
+                const int b = __ldg(&bin_mapping[pix]);
+                if (b < 0 || b >= nb) continue;
+                const T vl = RN<T>::add(RN<T>::add(RN<T>::mul(G.rot[6], vx), RN<T>::mul(G.rot[7], vy)), RN<T>::mul(G.rot[8], vz));
+                const T s_b = T(__ldg(&sg[b]));
+                const T yv = (vl * kms - T(__ldg(&v0g[b]))) / s_b;
+                const T gw = w * isq2pi / s_b * M<T>::exp(T(-0.5) * yv * yv);
+                const T H1 = sq2 * yv;
+                const T H2 = (sq2 * yv * H1 - T(1)) * isq2;
+                const T H3 = (sq2 * yv * H2 - sq2 * H1) * isq3;
+                const T H4 = (sq2 * yv * H3 - sq3 * H2) * T(0.5);
+                atomicAdd(&acc[off_xy + b], w);
+                atomicAdd(&acc[off_h + b], gw);
+                atomicAdd(&acc[off_h + nb + b], gw * H1);
+                atomicAdd(&acc[off_h + 2 * nb + b], gw * H2);
+                atomicAdd(&acc[off_h + 3 * nb + b], gw * H3);
+                atomicAdd(&acc[off_h + 4 * nb + b], gw * H4);
+            }
+        }
+    }
+    __syncthreads();
+    T *col = library + (int64_t)p * G.rows;
+    for (int i = threadIdx.x; i < G.rows; i += blockDim.x) {
+        T v = acc[i];
+        if (i >= off_xy && i < off_h) v = T((double)v / (num_per_bin[i - off_xy] * area_pixel + kEps));
+        col[i] = v;
+    }
+}
+
+template <typename T>
+static int launch(const smx_binning *g, const void *samples, const int32_t *n_stored, int64_t slots,
+                  const void *info, const void *t_total, const int32_t *bin_mapping, const double *num_per_bin,
+                  const double *v0, const double *s, void *library, int8_t *valid, cudaStream_t st) {
+    GeoT<T> G;
+    const double lo[3] = {g->R_lo, g->z_lo, g->phi_lo}, hi[3] = {g->R_hi, g->z_hi, g->phi_hi};
+    const int n[3] = {g->nR, g->nz, g->nphi};
+    for (int d = 0; d < 3; ++d) {
+        G.lo[d] = T(lo[d]);
+        G.span[d] = T(hi[d]) - T(lo[d]);
+        G.fn[d] = T(n[d]);
+        G.n[d] = n[d];
+    }
+    const double xlo[2] = {g->X_lo, g->Y_lo}, xhi[2] = {g->X_hi, g->Y_hi};
+    const int nx[2] = {g->nX, g->nY};
+    for (int d = 0; d < 2; ++d) {
+        G.xlo[d] = T(xlo[d]);
+        G.xspan[d] = T(xhi[d]) - T(xlo[d]);
+        G.xfn[d] = T(nx[d]);
+        G.nx[d] = nx[d];
+    }
+    for (int i = 0; i < 9; ++i) G.rot[i] = T(g->rot[i]);
+    G.n_cells = g->nR * g->nz * g->nphi;
+    G.n_pix = g->nX * g->nY;
+    G.n_bins = g->n_bins;
+    G.rows = G.n_cells + 6 * g->n_bins;
+    G.n_part = g->n_part;
+    G.n_real = g->n_real;
+    G.symmetry = g->symmetry;
+    const size_t smem = (size_t)G.rows * sizeof(T);
+    int dev = 0, max_smem = 0;
+    SMX_TRY_CUDA(cudaGetDevice(&dev));
+    SMX_TRY_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    if (smem + 1024 > (size_t)max_smem)
+        return set_error(SMX_ERR_UNSUPPORTED, "library row of %d entries does not fit in shared memory", G.rows);
+    SMX_TRY_CUDA(cudaFuncSetAttribute(project_bin_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const double area = ((g->X_hi - g->X_lo) / g->nX) * ((g->Y_hi - g->Y_lo) / g->nY) * 1e6;
+    project_bin_kernel<T><<<g->n_part, 256, smem, st>>>(G, (const T *)samples, n_stored, slots, (const T *)info,
+                                                        (const T *)t_total, bin_mapping, num_per_bin, v0, s, area,
+                                                        (T *)library, valid);
+    SMX_TRY_CUDA(cudaGetLastError());
+    return SMX_OK;
+}
+
+}  // namespace smx
+
+using namespace smx;
+
+extern "C" int smx_project_bin(const smx_binning *geo, int precision, const void *samples, const int32_t *n_stored,
+                               int64_t slots, const void *info, const void *t_total, const int32_t *bin_mapping,
+                               const double *num_per_bin, const double *v0, const double *s, void *library,
+                               int8_t *valid, void *stream) {
+    if (!geo) return set_error(SMX_ERR_ARGUMENT, "smx_project_bin: geometry is NULL");
+    if (geo->n_part < 0 || geo->n_real < 1 || geo->n_real > 8 || geo->nR < 1 || geo->nz < 1 || geo->nphi < 1 ||
+        geo->nX < 1 || geo->nY < 1 || geo->n_bins < 1 || slots < 1)
+        return set_error(SMX_ERR_ARGUMENT, "smx_project_bin: bad sizes (n_real must be 1..8)");
+    if (!(geo->R_hi > geo->R_lo) || !(geo->z_hi > geo->z_lo) || !(geo->phi_hi > geo->phi_lo) ||
+        !(geo->X_hi > geo->X_lo) || !(geo->Y_hi > geo->Y_lo))
+        return set_error(SMX_ERR_ARGUMENT, "smx_project_bin: empty grid range");
+    if (geo->n_part == 0) return SMX_OK;
+    if (!samples || !n_stored || !info || !t_total || !bin_mapping || !num_per_bin || !v0 || !s || !library)
+        return set_error(SMX_ERR_ARGUMENT, "smx_project_bin: NULL buffer");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (precision == SMX_FP32)
+        return launch<float>(geo, samples, n_stored, slots, info, t_total, bin_mapping, num_per_bin, v0, s, library,
+                             valid, st);
+    if (precision == SMX_FP64)
+        return launch<double>(geo, samples, n_stored, slots, info, t_total, bin_mapping, num_per_bin, v0, s, library,
+                              valid, st);
+    return set_error(SMX_ERR_ARGUMENT, "bad precision %d", precision);
+}

@@ -1,0 +1,341 @@
+// Internal definitions shared by the SchwarMAX GB300 kernels.
+//
+// The canonical potential (likelihood.py:13-71) is evaluated inline with an
+// analytic gradient.  For the Dehnen & Aly needle terms the gradient follows
+// from the A/B/Ax recurrence (dehnen_bar.py:104-157) differentiated by hand:
+//   d A_n/d x = Ax_n,  d C_n/d x = A_n           (C_n = x A_n - B_n)
+//   d/du2 of  A_{n+2} = ((n-1) A_n + x Ax_n)/(n u2),  B_{n+2} = -Ax_n/n,
+//   Ax_n = R2^{-n/2}  =>  d Ax_n/d u2 = -(n/2) Ax_n / R2
+// with u2 = y^2 + Z^2 and Z = sqrt(z^2 + b^2) + a.  The n = 1 terms use
+// cancellation-free forms: A_1 = log(x + r) = log(u2 / (r - x)) for x < 0, and
+// the needle difference A_1(x+L) - A_1(x-L) = log1p(2L (1 + 2|x|/(r+ + r-)) / D).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/schwarmax.h"
+
+namespace smx {
+
+constexpr double kG = 4.498502151469554e-06;          // kpc^3 / Msun / Gyr^2
+constexpr double kKpcGyrToKms = 0.9777922216807892;
+constexpr double kEps = 1e-12;                         // EPSILON of constants.py:11
+constexpr double kPi = 3.14159265358979323846;
+
+int set_error(int status, const char *fmt, ...);
+int check_cuda(cudaError_t e, const char *what);
+void clear_error();
+
+#define SMX_TRY_CUDA(expr)                                              \
+    do {                                                                \
+        cudaError_t _e = (expr);                                        \
+        if (_e != cudaSuccess) return ::smx::check_cuda(_e, #expr);     \
+    } while (0)
+
+// ---------------------------------------------------------------- math
+template <typename T> struct M;
+template <> struct M<float> {
+    static __device__ __forceinline__ float rsqrt(float x) { return rsqrtf(x); }
+    static __device__ __forceinline__ float sqrt(float x) { return sqrtf(x); }
+    static __device__ __forceinline__ float log(float x) { return logf(x); }
+    static __device__ __forceinline__ float log1p(float x) { return log1pf(x); }
+    static __device__ __forceinline__ float rcbrt(float x) { return rcbrtf(x); }
+    static __device__ __forceinline__ float exp(float x) { return expf(x); }
+    static __device__ __forceinline__ float atan2(float y, float x) { return atan2f(y, x); }
+    static __device__ __forceinline__ float abs(float x) { return fabsf(x); }
+};
+template <> struct M<double> {
+    static __device__ __forceinline__ double rsqrt(double x) { return ::rsqrt(x); }
+    static __device__ __forceinline__ double sqrt(double x) { return ::sqrt(x); }
+    static __device__ __forceinline__ double log(double x) { return ::log(x); }
+    static __device__ __forceinline__ double log1p(double x) { return ::log1p(x); }
+    static __device__ __forceinline__ double rcbrt(double x) { return ::rcbrt(x); }
+    static __device__ __forceinline__ double exp(double x) { return ::exp(x); }
+    static __device__ __forceinline__ double atan2(double y, double x) { return ::atan2(y, x); }
+    static __device__ __forceinline__ double abs(double x) { return ::fabs(x); }
+};
+
+// -------------------------------------------------------- potential params
+template <typename T> struct PotT {
+    T GMh, iRs, iqa2, iqb2, iqc2;                 // NFW
+    T GMd, Md, ad, bd2;                            // Miyamoto-Nagai
+    T ba, bb2, bL, bc1, bc2;                       // T3 bar: c1 = M(1-g)/(2L), c2 = M g/L^2
+    T ua, ub2, uL, uc1, uc2;                       // V4 bulge
+};
+
+template <typename T> inline PotT<T> make_pot(const smx_potential &p) {
+    PotT<T> q;
+    q.GMh = T(kG * p.halo_M);
+    q.iRs = T(1.0 / p.halo_Rs);
+    q.iqa2 = T(1.0 / (p.halo_qa * p.halo_qa));
+    q.iqb2 = T(1.0 / (p.halo_qb * p.halo_qb));
+    q.iqc2 = T(1.0 / (p.halo_qc * p.halo_qc));
+    q.GMd = T(kG * p.disc_M);
+    q.Md = T(p.disc_M);
+    q.ad = T(p.disc_a);
+    q.bd2 = T(p.disc_b * p.disc_b);
+    q.ba = T(p.bar_a);
+    q.bb2 = T(p.bar_b * p.bar_b);
+    q.bL = T(p.bar_L);
+    q.bc1 = T(p.bar_M * (1.0 - p.bar_gamma) / (2.0 * p.bar_L));
+    q.bc2 = T(p.bar_M * p.bar_gamma / (p.bar_L * p.bar_L));
+    q.ua = T(p.bulge_a);
+    q.ub2 = T(p.bulge_b * p.bulge_b);
+    q.uL = T(p.bulge_L);
+    q.uc1 = T(p.bulge_M * (1.0 - p.bulge_gamma) / (2.0 * p.bulge_L));
+    q.uc2 = T(p.bulge_M * p.bulge_gamma / (p.bulge_L * p.bulge_L));
+    return q;
+}
+
+int validate_potential(const smx_potential *p);
+
+// ------------------------------------------------------------ needle sums
+// Running state of the recurrence at one needle position xp.
+template <typename T, bool GRAD> struct Rec {
+    T xp, R2, iR2, r, ir;
+    T A, B, Ax, Au, Bu, Axu;   // current order n
+    __device__ __forceinline__ void init(T xp_, T u2, T iu2) {
+        xp = xp_;
+        R2 = xp * xp + u2;
+        ir = M<T>::rsqrt(R2);
+        iR2 = ir * ir;
+        r = R2 * ir;
+        A = T(0);          // A_1 = log term is supplied separately when needed
+        B = r;
+        Ax = ir;
+        if (GRAD) {
+            // d A_1 / d u2 = 1/(2 r (xp + r)); (xp + r) = u2/(r - xp) for xp < 0
+            Au = (xp >= T(0)) ? T(0.5) * ir / (xp + r) : T(0.5) * ir * (r - xp) * iu2;
+            Bu = T(0.5) * ir;
+            Axu = T(-0.5) * ir * iR2;
+        }
+    }
+    __device__ __forceinline__ T log_A1(T u2) const {
+        return (xp >= T(0)) ? M<T>::log(xp + r) : M<T>::log(u2 / (r - xp));
+    }
+    // advance n -> n + 2
+    __device__ __forceinline__ void step(int n, T iu2) {
+        const T tn = T(n);
+        const T inv_n = T(1) / tn;
+        T An = ((tn - T(1)) * A + xp * Ax) * iu2 * inv_n;
+        T Bn = -Ax * inv_n;
+        if (GRAD) {
+            T Aun = ((tn - T(1)) * Au + xp * Axu) * iu2 * inv_n - An * iu2;
+            Bu = -Axu * inv_n;
+            Au = Aun;
+        }
+        Ax = Ax * iR2;
+        if (GRAD) Axu = T(-0.5) * T(n + 2) * Ax * iR2;
+        A = An;
+        B = Bn;
+    }
+};
+
+// Sum over orders n = 1, 3, ..., 2K-1 of kc[k] F_n, where
+// F_n = c1 [A_n(x+L) - A_n(x-L)] + c2 [C_n(x+L) + C_n(x-L) - 2 C_n(x)]
+// (dehnen_bar.py:211-241).  With GRAD also returns sum kc Fx_n (d/dx),
+// sum kc Fu_n (d/du2) and sum dkc F_n.  FIRST = index of the first order with
+// a non-zero coefficient (orders below it are skipped, so n = 1 logs are
+// only evaluated when needed).
+template <typename T, int K, int FIRST, bool GRAD>
+__device__ __forceinline__ void needle_sum(T x, T u2, T L, T c1, T c2, const T (&kc)[K],
+                                           const T (&dkc)[K], T &S0, T &Sx, T &Su, T &SZ) {
+    const T iu2 = T(1) / u2;
+    S0 = Sx = Su = SZ = T(0);
+    if (c1 != T(0)) {
+        Rec<T, GRAD> p, m;
+        p.init(x + L, u2, iu2);
+        m.init(x - L, u2, iu2);
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            if (k >= FIRST) {
+                T F;
+                if (k == 0) {
+                    const T ax = M<T>::abs(x);
+                    const T D = (x >= T(0)) ? (m.xp + m.r) : (p.r - p.xp);
+                    F = c1 * M<T>::log1p(T(2) * L * (T(1) + T(2) * ax / (p.r + m.r)) / D);
+                } else {
+                    F = c1 * (p.A - m.A);
+                }
+                S0 += kc[k] * F;
+                if (GRAD) {
+                    Sx += kc[k] * (c1 * (p.Ax - m.Ax));
+                    Su += kc[k] * (c1 * (p.Au - m.Au));
+                    SZ += dkc[k] * F;
+                }
+            }
+            if (k + 1 < K) {
+                p.step(2 * k + 1, iu2);
+                m.step(2 * k + 1, iu2);
+            }
+        }
+    }
+    if (c2 != T(0)) {
+        Rec<T, GRAD> p, m, o;
+        p.init(x + L, u2, iu2);
+        m.init(x - L, u2, iu2);
+        o.init(x, u2, iu2);
+        if (FIRST == 0) {
+            p.A = p.log_A1(u2);
+            m.A = m.log_A1(u2);
+            o.A = o.log_A1(u2);
+        }
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            if (k >= FIRST) {
+                const T Cp = p.xp * p.A - p.B, Cm = m.xp * m.A - m.B, Co = o.xp * o.A - o.B;
+                const T F = c2 * (Cp + Cm - T(2) * Co);
+                S0 += kc[k] * F;
+                if (GRAD) {
+                    Sx += kc[k] * (c2 * (p.A + m.A - T(2) * o.A));
+                    const T Cup = p.xp * p.Au - p.Bu, Cum = m.xp * m.Au - m.Bu, Cuo = o.xp * o.Au - o.Bu;
+                    Su += kc[k] * (c2 * (Cup + Cum - T(2) * Cuo));
+                    SZ += dkc[k] * F;
+                }
+            }
+            if (k + 1 < K) {
+                // (n-1) A_n vanishes at n = 1, so the log term never feeds n >= 3
+                p.step(2 * k + 1, iu2);
+                m.step(2 * k + 1, iu2);
+                o.step(2 * k + 1, iu2);
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------- potential
+// Phi and/or its gradient (dPhi/dx, ...) of the canonical model at (x, y, z).
+template <typename T, bool WANT_PHI, bool WANT_GRAD>
+__device__ __forceinline__ void potential(const PotT<T> &P, T x, T y, T z, T &phi, T &gx, T &gy, T &gz) {
+    const T G = T(kG);
+    const T eps = T(kEps);
+    phi = gx = gy = gz = T(0);
+    {   // NFW halo (potentials.py:18-27)
+        const T s2 = x * x * P.iqa2 + y * y * P.iqb2 + z * z * P.iqc2 + eps;
+        const T ir = M<T>::rsqrt(s2);
+        const T r = s2 * ir;
+        const T q = r * P.iRs;
+        const T l = M<T>::log1p(q);
+        const T ire = T(1) / (r + eps);
+        if (WANT_PHI) phi += -P.GMh * l * ire;
+        if (WANT_GRAD) {
+            const T dpdr = -P.GMh * (P.iRs / (T(1) + q) - l * ire) * ire;
+            const T c = dpdr * ir;
+            gx += c * x * P.iqa2;
+            gy += c * y * P.iqb2;
+            gz += c * z * P.iqc2;
+        }
+    }
+    {   // Miyamoto-Nagai disc (potentials.py:51-65)
+        const T rx = x + eps, ry = y + eps, rz = z + eps;
+        const T zeta = M<T>::sqrt(rz * rz + P.bd2);
+        const T s = P.ad + zeta;
+        const T iD = M<T>::rsqrt(rx * rx + ry * ry + s * s);
+        if (WANT_PHI) phi += -P.GMd * iD;
+        if (WANT_GRAD) {
+            const T c = P.GMd * iD * iD * iD;
+            gx += c * rx;
+            gy += c * ry;
+            gz += c * s * rz / zeta;
+        }
+    }
+    {   // T3 bar (dehnen_bar.py:1318-1326)
+        const T a = P.ba;
+        const T ze = M<T>::sqrt(z * z + P.bb2);
+        const T Z = ze + a;
+        const T u2 = y * y + Z * Z;
+        const T aZ = a * Z;
+        const T kc[3] = {T(1), a * (Z - a / T(3)), aZ * aZ};
+        const T dk[3] = {T(0), a, T(2) * a * aZ};
+        T S0, Sx, Su, SZ;
+        needle_sum<T, 3, 0, WANT_GRAD>(x, u2, P.bL, P.bc1, P.bc2, kc, dk, S0, Sx, Su, SZ);
+        if (WANT_PHI) phi += -G * S0;
+        if (WANT_GRAD) {
+            gx += -G * Sx;
+            gy += -G * Su * T(2) * y;
+            gz += -G * (SZ + Su * T(2) * Z) * (z / ze);
+        }
+    }
+    {   // V4 bulge (dehnen_bar.py:1371-1383)
+        const T a = P.ua;
+        const T ze = M<T>::sqrt(z * z + P.ub2);
+        const T Z = ze + a;
+        const T u2 = y * y + Z * Z;
+        const T h = T(0.5) * P.ub2;
+        const T aZ = a * Z;
+        const T iz = T(1) / ze;
+        const T kc[5] = {T(1), a * (Z - T(0.4) * a) + h,
+                         T(3) * a * (T(0.2) * aZ * (Z + Z - a) + h * (Z - T(0.2) * a)),
+                         aZ * aZ * (aZ + T(6) * h), T(7) * h * aZ * aZ * aZ * Z * iz};
+        const T dk[5] = {T(0), a, T(3) * a * (T(0.2) * a * (T(4) * Z - a) + h),
+                         a * aZ * (T(3) * aZ + T(12) * h),
+                         T(7) * h * aZ * aZ * aZ * (T(3) * Z - T(4) * a) * iz * iz};
+        T S0, Sx, Su, SZ;
+        needle_sum<T, 5, 0, WANT_GRAD>(x, u2, P.uL, P.uc1, P.uc2, kc, dk, S0, Sx, Su, SZ);
+        if (WANT_PHI) phi += -G * S0;
+        if (WANT_GRAD) {
+            gx += -G * Sx;
+            gy += -G * Su * T(2) * y;
+            gz += -G * (SZ + Su * T(2) * Z) * (z / ze);
+        }
+    }
+}
+
+// Stellar density MN + T3 + V4 (potentials.py:29-49, dehnen_bar.py:1425-1438, 1526-1543).
+template <typename T>
+__device__ __forceinline__ T density(const PotT<T> &P, T x, T y, T z) {
+    const T eps = T(kEps);
+    const T pi = T(kPi);
+    T rho;
+    {
+        const T rx = x + eps, ry = y + eps, rz = z + eps;
+        const T R2 = rx * rx + ry * ry;
+        const T beta = M<T>::sqrt(rz * rz + P.bd2);
+        const T ab = P.ad + beta;
+        const T D2 = R2 + ab * ab;
+        const T num = P.ad * R2 + (P.ad + T(3) * beta) * ab * ab;
+        const T den = beta * beta * beta * D2 * D2 * M<T>::sqrt(D2);
+        rho = (P.bd2 * P.Md / (T(4) * pi)) * (num / den);
+    }
+    {   // T3: orders 5, 7, 9 -> K = 5, first used index 2
+        const T a = P.ba, b2 = P.bb2;
+        const T ze = M<T>::sqrt(z * z + b2);
+        const T iz = T(1) / ze;
+        const T Z = ze + a;
+        const T Z2 = Z * Z, A2 = a * a;
+        const T u2 = y * y + Z2;
+        const T kc[5] = {T(0), T(0), T(3) * ze * ze * ze, T(5) * a * Z2 * ((T(3) * ze - T(2) * a) * ze + A2),
+                         T(35) * A2 * Z2 * Z2 * ze};
+        const T dk[5] = {T(0), T(0), T(0), T(0), T(0)};
+        T S0, Sx, Su, SZ;
+        needle_sum<T, 5, 2, false>(x, u2, P.bL, P.bc1, P.bc2, kc, dk, S0, Sx, Su, SZ);
+        rho += (b2 * iz * iz * iz) * (T(0.25) / pi) * S0;
+    }
+    {   // V4: orders 7, 9, 11, 13 -> K = 7, first used index 3
+        const T a = P.ua, b2 = P.ub2;
+        const T ze = M<T>::sqrt(z * z + b2);
+        const T iz = T(1) / ze;
+        const T Z = ze + a;
+        const T Z2 = Z * Z, A2 = a * a, AZ = a * Z;
+        const T u2 = y * y + Z2;
+        const T kc[7] = {T(0), T(0), T(0), T(5) * ze * ze * ze,
+                         T(7) * a * Z2 * (T(5) * ze * ze - T(4) * a * ze + T(3) * A2 - T(2) * a * A2 * iz + A2 * A2 * iz * iz),
+                         T(63) * A2 * Z2 * Z2 * (ze + ze - T(2) * a + A2 * iz),
+                         T(231) * A2 * AZ * Z2 * Z2 * Z};
+        const T dk[7] = {T(0), T(0), T(0), T(0), T(0), T(0), T(0)};
+        T S0, Sx, Su, SZ;
+        needle_sum<T, 7, 3, false>(x, u2, P.uL, P.uc1, P.uc2, kc, dk, S0, Sx, Su, SZ);
+        rho += (b2 * iz * iz * iz) * (T(0.375) * b2 / pi) * S0;
+    }
+    return rho;
+}
+
+template <typename T>
+__device__ __forceinline__ T phi_only(const PotT<T> &P, T x, T y, T z) {
+    T p, a, b, c;
+    potential<T, true, false>(P, x, y, z, p, a, b, c);
+    return p;
+}
+
+}  // namespace smx

@@ -1,0 +1,315 @@
+"""Device-side pipeline of one model evaluation.
+
+ICs (Jeans + V_c + T_orb + jitter) -> orbits -> projection/binning -> 3-D
+target -> data scaling and gamma_kin -> bootstrap ADMM NNLS -> model maps and
+chi^2.  Mirrors build_model (model.py:70-286) and the chi^2 of
+model_likelihood (likelihood.py:192-244).  All arrays live on the GPU; the host
+only forms small parameter structs and launches.
+
+Random draws are inputs: dict_data may carry 'jeans_normals' (3, n) and
+'jitter_uniforms' (6, n, n_real) in place of the reference's threefry keys
+42/109/2026 and 911 (model.py:112-138).  When they are absent they are drawn
+once from NumPy generators seeded with the same numbers.
+"""
+import math
+from dataclasses import dataclass, field, replace
+
+import numpy as np
+import torch
+
+from . import kernels
+from ._lib import SMX_MODE_REFERENCE, SMX_MODE_SAMPLED, SmxBinning, SmxIntegrator
+from .potentials import potential_struct
+
+EPSILON = 1e-12
+KPCGYR_TO_KMS = 0.9777922216807892
+
+
+@dataclass
+class Settings:
+    """Integrator and precision settings.  Defaults are the reference's
+    hard-coded values (model.py:127, 163-169)."""
+    n_real: int = 4
+    mode: str = "reference"          # "reference" (N_max attempts) or "sampled"
+    n_attempts: int = 5000
+    n_periods: float = 50.0
+    steps_per_period: float = 100.0
+    atol: float = 1e-7
+    rtol: float = 1e-4
+    dt_min: float = 1e-5
+    dt_max: float = 0.3
+    n_samples: int = 1000
+    max_attempts: int = 1_000_000
+    bulge_mass: float = None
+    precision: str = "mixed"         # "mixed" (FP32 orbits, TF32/FP64 NNLS) or "fp64"
+
+    @property
+    def dtype(self):
+        return torch.float32 if self.precision == "mixed" else torch.float64
+
+    @property
+    def slots(self):
+        return self.n_attempts if self.mode == "reference" else self.n_samples
+
+
+def settings_from(settings=None, **kw):
+    s = Settings() if settings is None else (replace(settings) if isinstance(settings, Settings) else Settings(**settings))
+    return replace(s, **{k: v for k, v in kw.items() if v is not None})
+
+
+def _np(x, dtype=np.float64):
+    if isinstance(x, torch.Tensor):
+        return x.detach().cpu().numpy().astype(dtype)
+    return np.asarray(x, dtype=dtype)
+
+
+def default_draws(n, n_real):
+    """Seeded stand-ins for the threefry draws of model.py:112-138."""
+    normals = np.stack([np.random.default_rng(k).standard_normal(n) for k in (42, 109, 2026)])
+    uniforms = np.random.default_rng(911).random((6, n, n_real))
+    return normals, uniforms
+
+
+class DeviceData:
+    """dict_data (utils.py:688-741 schema) on the device."""
+
+    def __init__(self, dict_data, device="cuda", n_real=4, pin=False):
+        d = dict_data
+        self.source = d
+
+        def dev(x, dtype=torch.float64):
+            a = torch.as_tensor(_np(x, np.float64 if dtype == torch.float64 else np.int32))
+            if pin:
+                a = a.pin_memory()
+            return a.to(device, dtype=dtype, non_blocking=pin).contiguous()
+
+        w0 = _np(d["w0"])
+        self.n = w0.shape[0]
+        if "jeans_normals" in d and "jitter_uniforms" in d:
+            normals, uniforms = _np(d["jeans_normals"]), _np(d["jitter_uniforms"])
+        else:
+            normals, uniforms = default_draws(self.n, max(n_real, 1))
+        self.uniforms_traj = _np(d["jitter_uniforms_traj"]) if "jitter_uniforms_traj" in d else None
+        self.pos64 = dev(w0.T.copy())
+        self.normals64 = dev(normals)
+        self.uniforms64 = dev(uniforms)
+        self.bin_mapping = dev(d["bin_mapping"], torch.int32)
+        self.num_per_bin = dev(d["num_per_bin"])
+        self.v0 = dev(d["v0"])
+        self.s = dev(d["s"])
+        self.n_bins = int(self.v0.numel())
+        self.R_grid, self.z_grid, self.phi_grid = dev(d["R_grid"]), dev(d["z_grid"]), dev(d["phi_grid"])
+        self.dR, self.dz, self.dphi = float(_np(d["dR"])), float(_np(d["dz"])), float(_np(d["dphi"]))
+        self.sample = dev(d["sample_for_integration"])
+        self.xy = dev(d["XY_density_data"])
+        self.xy_err = dev(d["XY_density_data_err"])
+        self.h = torch.stack([dev(d[f"h{k}_data"]) for k in range(1, 5)])
+        self.h_err = torch.stack([dev(d[f"h{k}_data_err"]) for k in range(1, 5)])
+        self.N_xy = dev(d["XY_standard_normal"])
+        self.N_h = torch.stack([dev(d[f"h{k}_standard_normal"]) for k in range(1, 5)])
+        self.n_boot = int(self.N_xy.shape[0])
+        X, Y, nXY = _np(d["X_minmax"]), _np(d["Y_minmax"]), _np(d["nX_nY"])
+        self.area_pixel = ((X[1] - X[0]) / nXY[0]) * ((Y[1] - Y[0]) / nXY[1]) * 1e6
+        self._cast = {}
+
+    def cast(self, dtype, n_real):
+        key = (dtype, n_real)
+        if key not in self._cast:
+            uni = self.uniforms64[:, :, :n_real]
+            self._cast[key] = (self.pos64.to(dtype).contiguous(), self.normals64.to(dtype).contiguous(),
+                               uni.to(dtype).contiguous())
+        return self._cast[key]
+
+    def traj_uniforms(self, dtype):
+        if self.uniforms_traj is not None:
+            return torch.as_tensor(self.uniforms_traj, dtype=dtype, device=self.pos64.device).contiguous()
+        return self.uniforms64[:, :, :1].to(dtype).contiguous()
+
+
+_device_cache = []
+
+
+def device_data(dict_data, n_real=4, cache=True):
+    if isinstance(dict_data, DeviceData):
+        return dict_data
+    if cache:
+        for src, dd in _device_cache:
+            if src is dict_data:
+                return dd
+    dd = DeviceData(dict_data, n_real=n_real)
+    if cache:
+        _device_cache.append((dict_data, dd))
+        if len(_device_cache) > 4:
+            _device_cache.pop(0)
+    return dd
+
+
+@dataclass
+class Grid:
+    n_rzphi: tuple
+    rzphi_lim: np.ndarray
+    xy_lim: np.ndarray
+    n_xy: tuple
+
+    @property
+    def n_cells(self):
+        return int(np.prod(self.n_rzphi))
+
+
+_buffers = {}
+
+
+def _integrator_buffers(n_orb, slots, dtype):
+    key = (n_orb, slots, dtype)
+    b = _buffers.get(key)
+    if b is None:
+        _buffers.clear()
+        b = kernels.IntegratorBuffers(n_orb, slots, dtype, torch.device("cuda"))
+        _buffers[key] = b
+    return b
+
+
+def build_library(pot, params_disk_rho, dd: DeviceData, grid: Grid, st: Settings, trajectory=False):
+    """Returns dict(library (n, rows), ic, bufs, valid)."""
+    dtype = st.dtype
+    n_real = 1 if trajectory else st.n_real
+    pos, normals, uni = dd.cast(dtype, st.n_real)
+    if trajectory:
+        uni = dd.traj_uniforms(dtype)
+    ic = kernels.initial_conditions(pot, pos, normals, uni, n_real, st.n_periods, st.steps_per_period)
+    mode = "reference" if trajectory else st.mode
+    cfg = SmxIntegrator(mode=SMX_MODE_REFERENCE if mode == "reference" else SMX_MODE_SAMPLED,
+                        store_all=1 if trajectory else 0, n_attempts=st.n_attempts, n_samples=st.n_samples,
+                        max_attempts=st.max_attempts, atol=st.atol, rtol=st.rtol, dt_min=st.dt_min,
+                        dt_max=st.dt_max, omega=-float(params_disk_rho["Omega_bar"]))
+    slots = st.n_attempts if mode == "reference" else st.n_samples
+    bufs = _integrator_buffers(dd.n * n_real, slots, dtype)
+    kernels.integrate(pot, cfg, ic["w0"], ic["dt_init"], ic["t_total"], bufs)
+    geo = binning_geometry(params_disk_rho, grid, dd, n_real, symmetry=0 if trajectory else 1)
+    valid = torch.empty(dd.n * n_real, dtype=torch.int8, device="cuda")
+    lib = kernels.project_bin(geo, bufs, ic["t_total"], dd.bin_mapping, dd.num_per_bin, dd.v0, dd.s, valid=valid)
+    return dict(library=lib, ic=ic, bufs=bufs, valid=valid, geo=geo)
+
+
+def rotation_matrix(alpha_deg, beta_deg, gamma_deg):
+    """makeRotationMatrix (utils.py:164-179): (Rz(g) Rx(b) Rz(a))^T, X = R @ x."""
+    a, b, g = (math.radians(float(v)) for v in (alpha_deg, beta_deg, gamma_deg))
+
+    def Rz(t):
+        c, s = math.cos(t), math.sin(t)
+        return np.array([[c, -s, 0.0], [s, c, 0.0], [0.0, 0.0, 1.0]])
+
+    def Rx(t):
+        c, s = math.cos(t), math.sin(t)
+        return np.array([[1.0, 0.0, 0.0], [0.0, c, -s], [0.0, s, c]])
+
+    return (Rz(g) @ Rx(b) @ Rz(a)).T
+
+
+def binning_geometry(params_disk_rho, grid: Grid, dd: DeviceData, n_real, symmetry=1):
+    rot = rotation_matrix(params_disk_rho["alpha"], params_disk_rho["beta"], params_disk_rho["gamma"])
+    lim = np.asarray(grid.rzphi_lim, dtype=np.float64)
+    xl = np.asarray(grid.xy_lim, dtype=np.float64)
+    nR, nz, nphi = (int(v) for v in grid.n_rzphi)
+    nX, nY = (int(v) for v in grid.n_xy)
+    g = SmxBinning(n_part=dd.n, n_real=n_real, nR=nR, nz=nz, nphi=nphi, R_lo=lim[0, 0], R_hi=lim[0, 1],
+                   z_lo=lim[1, 0], z_hi=lim[1, 1], phi_lo=lim[2, 0], phi_hi=lim[2, 1], nX=nX, nY=nY,
+                   X_lo=xl[0, 0], X_hi=xl[0, 1], Y_lo=xl[1, 0], Y_hi=xl[1, 1], n_bins=dd.n_bins, symmetry=symmetry)
+    for i in range(9):
+        g.rot[i] = float(rot.reshape(-1)[i])
+    return g
+
+
+_rowmaps = {}
+
+
+def row_map(n_cells, nb):
+    key = (n_cells, nb)
+    if key not in _rowmaps:
+        idx = [np.arange(n_cells), n_cells + np.arange(nb)]
+        for k in range(1, 5):
+            idx.append(n_cells + (1 + k) * nb + np.arange(nb))
+        _rowmaps[key] = torch.as_tensor(np.concatenate(idx).astype(np.int32), device="cuda")
+    return _rowmaps[key]
+
+
+def data_terms(dd: DeviceData, params_disk_rho, y_rz_raw, n_orb):
+    """Target normalisation, data scaling and gamma_kin (model.py:213-258)."""
+    l2m = 1.0 / float(params_disk_rho["mass_to_light_ratio"])
+    y_rz = y_rz_raw.to(torch.float64)
+    sig_rz = 0.02 * y_rz + 1e-10
+    y_xy = dd.xy / l2m
+    sig_xy = (dd.xy_err + EPSILON) / l2m
+    sh = dd.h_err + EPSILON
+    mmpo = y_rz.sum() / n_orb
+    y_xy, sig_xy, y_rz, sig_rz = y_xy / mmpo, sig_xy / mmpo, y_rz / mmpo, sig_rz / mmpo
+    M_b = y_xy * dd.num_per_bin * dd.area_pixel
+    normGH = 1.0 + dd.h[3] * math.sqrt(6.0) / 4.0
+    gamma = M_b / (normGH * 2.0 * math.sqrt(math.pi) * dd.s + EPSILON)
+    return dict(y_rz=y_rz, sig_rz=sig_rz, y_xy=y_xy, sig_xy=sig_xy, sh=sh, mmpo=mmpo, gamma=gamma, l2m=l2m)
+
+
+def nnls_inputs(d, dd: DeviceData, n_cells, weights, boot=True, sig_xy=None, sig_h=None):
+    """row_scale (m,) and scaled data Y (B, m) of nnls.py:19-33 / 107-140."""
+    w_rz, w_xy, w_h = weights
+    sig_xy = d["sig_xy"] if sig_xy is None else sig_xy
+    sig_h = d["sh"] if sig_h is None else sig_h
+    g = torch.where(d["gamma"].abs() > 1e-8, d["gamma"], torch.full_like(d["gamma"], 1e-8))
+    rs = [w_rz / (d["sig_rz"] + 1e-8), w_xy / (sig_xy + 1e-8)]
+    rs += [w_h / (g * (sig_h[k] + 1e-8)) for k in range(4)]
+    row_scale = torch.cat(rs).contiguous()
+    if boot:
+        y_xy_b = d["y_xy"][None] + dd.N_xy * d["sig_xy"][None]
+        y_h_b = dd.h[:, None, :] + dd.N_h * d["sh"][:, None, :]
+    else:
+        y_xy_b = d["y_xy"][None]
+        y_h_b = dd.h[:, None, :]
+    B = y_xy_b.shape[0]
+    parts = [(w_rz * d["y_rz"] / (d["sig_rz"] + 1e-8))[None].expand(B, -1),
+             w_xy * y_xy_b / (sig_xy + 1e-8)[None]]
+    parts += [w_h * y_h_b[k] / (sig_h[k] + 1e-8)[None] for k in range(4)]
+    Y = torch.cat(parts, dim=1).contiguous()
+    return row_scale, Y
+
+
+def likelihood_data(dd: DeviceData):
+    """Raw bootstrap data of likelihood.py:199-211."""
+    sxy = dd.xy_err + EPSILON
+    sh = dd.h_err + EPSILON
+    y_xy_b = (dd.xy[None] + dd.N_xy * sxy[None]).contiguous()
+    y_h_b = (dd.h[:, None, :] + dd.N_h * sh[:, None, :]).contiguous()
+    return y_xy_b, y_h_b, sh.contiguous()
+
+
+def evaluate(pot, params_disk_rho, dd: DeviceData, grid: Grid, st: Settings, nnls_maxiter=200,
+             regularization=1.0, weights=(math.sqrt(5.0), math.sqrt(5.0), 1.0), sigma_amplify=1.0,
+             trajectory=False, want_maps=True):
+    """One model evaluation on the device.  Returns a dict of device tensors."""
+    libd = build_library(pot, params_disk_rho, dd, grid, st, trajectory=trajectory)
+    lib = libd["library"]
+    n = lib.shape[0]
+    nc = grid.n_cells
+    nb = dd.n_bins
+    y_rz_raw = kernels.density_target(pot, st.dtype, dd.R_grid, dd.z_grid, dd.phi_grid, dd.dR, dd.dz, dd.dphi,
+                                      dd.sample)
+    d = data_terms(dd, params_disk_rho, y_rz_raw, n)
+    row_scale, Y = nnls_inputs(d, dd, nc, weights)
+    # w = z = sum(y_Rzphi)/n at the start (nnls.py:122); read back with mmpo in one copy
+    host = torch.stack([d["y_rz"].sum() / n, d["mmpo"]]).cpu()
+    w_init, mmpo = float(host[0]), float(host[1])
+    W = kernels.nnls_admm(lib, row_map(nc, nb), row_scale, Y, nnls_maxiter, regularization, w_init,
+                          mixed=st.precision == "mixed")
+    y_xy_b, y_h_b, sh_raw = likelihood_data(dd)
+    maps, logl = kernels.model_maps(lib, nc, nb, W, d["gamma"].contiguous(), dd.v0, dd.s, d["y_rz"].contiguous(),
+                                    dd.xy, y_xy_b, y_h_b, sh_raw, mmpo * d["l2m"], sigma_amplify,
+                                    want_maps=want_maps)
+    return dict(lib=libd, data=d, W=W, maps=maps, logl=logl, n_cells=nc, n_bins=nb)
+
+
+def split_maps(maps, nc, nb):
+    o = dict(density_3d_model=maps[:, :nc], surface_density=maps[:, nc:nc + nb])
+    for k in range(4):
+        o[f"h{k + 1}"] = maps[:, nc + (1 + k) * nb: nc + (2 + k) * nb]
+    o["V"] = maps[:, nc + 5 * nb: nc + 6 * nb]
+    o["sigma"] = maps[:, nc + 6 * nb: nc + 7 * nb]
+    return o

@@ -1,0 +1,203 @@
+"""Typed wrappers over the C ABI for device tensors.
+
+Each function takes CUDA torch tensors, checks device, dtype, shape and
+contiguity, and launches the matching ``smx_*`` entry point on the current
+torch stream.  Nothing here computes on the host: a missing library or a CPU
+tensor is an error.
+"""
+import ctypes
+
+import torch
+
+from . import _lib
+from ._lib import (SmxBinning, SmxIntegrator, SmxMapsProblem, SmxNnlsProblem, SmxPotential, call)
+
+DTYPES = {torch.float32: _lib.SMX_FP32, torch.float64: _lib.SMX_FP64}
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _ptr(t):
+    return ctypes.c_void_p(0 if t is None else t.data_ptr())
+
+
+def _check(t, name, dtype=None, shape=None):
+    if t is None:
+        return
+    if not t.is_cuda:
+        raise ValueError(f"{name} must be a CUDA tensor (the library has no CPU path)")
+    if not t.is_contiguous():
+        raise ValueError(f"{name} must be contiguous")
+    if dtype is not None and t.dtype != dtype:
+        raise TypeError(f"{name} must be {dtype}, got {t.dtype}")
+    if shape is not None and tuple(t.shape) != tuple(shape):
+        raise ValueError(f"{name} must have shape {tuple(shape)}, got {tuple(t.shape)}")
+
+
+def _prec(dtype):
+    if dtype not in DTYPES:
+        raise TypeError(f"unsupported dtype {dtype}")
+    return DTYPES[dtype]
+
+
+def potential_eval(pot: SmxPotential, x, y, z, want_phi=True, want_acc=True, want_rho=False):
+    dt = x.dtype
+    n = x.numel()
+    for t, nm in ((x, "x"), (y, "y"), (z, "z")):
+        _check(t, nm, dt, (n,))
+    out = {}
+    phi = torch.empty(n, dtype=dt, device=x.device) if want_phi else None
+    acc = torch.empty(3, n, dtype=dt, device=x.device) if want_acc else None
+    rho = torch.empty(n, dtype=dt, device=x.device) if want_rho else None
+    call("smx_potential_eval", ctypes.byref(pot), _prec(dt), _ptr(x), _ptr(y), _ptr(z), n, _ptr(phi),
+         _ptr(acc[0] if want_acc else None), _ptr(acc[1] if want_acc else None), _ptr(acc[2] if want_acc else None),
+         _ptr(rho), _stream())
+    if want_phi:
+        out["phi"] = phi
+    if want_acc:
+        out["acc"] = acc
+    if want_rho:
+        out["rho"] = rho
+    return out
+
+
+def initial_conditions(pot, pos, normals, uniforms, n_real, n_periods, steps_per_period, extras=True):
+    """pos (3, n), normals (3, n), uniforms (6, n, n_real) -> dict of device tensors."""
+    dt = pos.dtype
+    n = pos.shape[1]
+    _check(pos, "pos", dt, (3, n))
+    _check(normals, "normals", dt, (3, n))
+    _check(uniforms, "uniforms", dt, (6, n, n_real))
+    dev = pos.device
+    w = torch.empty(6, n * n_real, dtype=dt, device=dev)
+    tt = torch.empty(n * n_real, dtype=dt, device=dev)
+    dt0 = torch.empty(n * n_real, dtype=dt, device=dev)
+    w0n = torch.empty(6, n, dtype=dt, device=dev) if extras else None
+    torb = torch.empty(n, dtype=dt, device=dev) if extras else None
+    vc = torch.empty(n, dtype=dt, device=dev) if extras else None
+    call("smx_initial_conditions", ctypes.byref(pot), _prec(dt), _ptr(pos), _ptr(normals), _ptr(uniforms), n,
+         n_real, float(n_periods), float(steps_per_period), _ptr(w), _ptr(tt), _ptr(dt0), _ptr(w0n), _ptr(torb),
+         _ptr(vc), _stream())
+    return dict(w0=w, t_total=tt, dt_init=dt0, w0_new=w0n, t_orb=torb, vc=vc)
+
+
+def density_target(pot, dtype, R_grid, z_grid, phi_grid, dR, dz, dphi, sample):
+    n = R_grid.numel()
+    for t, nm in ((R_grid, "R_grid"), (z_grid, "z_grid"), (phi_grid, "phi_grid")):
+        _check(t, nm, torch.float64, (n,))
+    _check(sample, "sample", torch.float64)
+    out = torch.empty(n, dtype=dtype, device=R_grid.device)
+    call("smx_density_target", ctypes.byref(pot), _prec(dtype), _ptr(R_grid), _ptr(z_grid), _ptr(phi_grid), n,
+         float(dR), float(dz), float(dphi), _ptr(sample), int(sample.shape[0]), _ptr(out), _stream())
+    return out
+
+
+class IntegratorBuffers:
+    """Sample store and per-orbit records for smx_integrate, reusable across calls."""
+
+    def __init__(self, n_orb, slots, dtype, device):
+        self.n_orb, self.slots, self.dtype = n_orb, slots, dtype
+        self.samples = torch.empty(7, n_orb, slots, dtype=dtype, device=device)
+        self.n_stored = torch.empty(n_orb, dtype=torch.int32, device=device)
+        self.info = torch.empty(_lib.INFO_FIELDS, n_orb, dtype=dtype, device=device)
+        self.status = torch.empty(n_orb, dtype=torch.int32, device=device)
+        self.queue = torch.zeros(1, dtype=torch.int32, device=device)
+
+
+def integrate(pot, cfg: SmxIntegrator, w0, dt_init, t_total, bufs: IntegratorBuffers):
+    dt = w0.dtype
+    n_orb = w0.shape[1]
+    _check(w0, "w0", dt, (6, n_orb))
+    _check(dt_init, "dt_init", dt, (n_orb,))
+    _check(t_total, "t_total", dt, (n_orb,))
+    if bufs.n_orb != n_orb or bufs.dtype != dt:
+        raise ValueError("integrator buffers do not match the orbits")
+    call("smx_integrate", ctypes.byref(pot), ctypes.byref(cfg), _prec(dt), _ptr(w0), _ptr(dt_init), _ptr(t_total),
+         n_orb, bufs.slots, _ptr(bufs.samples), _ptr(bufs.n_stored), _ptr(bufs.info), _ptr(bufs.status),
+         _ptr(bufs.queue), _stream())
+    return bufs
+
+
+def project_bin(geo: SmxBinning, bufs: IntegratorBuffers, t_total, bin_mapping, num_per_bin, v0, s, library=None,
+                valid=None):
+    dt = bufs.dtype
+    rows = geo.nR * geo.nz * geo.nphi + 6 * geo.n_bins
+    n_orb = geo.n_part * geo.n_real
+    if n_orb != bufs.n_orb:
+        raise ValueError("binning geometry does not match the integrated orbits")
+    _check(t_total, "t_total", dt, (n_orb,))
+    _check(bin_mapping, "bin_mapping", torch.int32, (geo.nX * geo.nY + 1,))
+    for t, nm in ((num_per_bin, "num_per_bin"), (v0, "v0"), (s, "s")):
+        _check(t, nm, torch.float64, (geo.n_bins,))
+    dev = bufs.samples.device
+    if library is None:
+        library = torch.empty(geo.n_part, rows, dtype=dt, device=dev)
+    _check(library, "library", dt, (geo.n_part, rows))
+    if valid is not None:
+        _check(valid, "valid", torch.int8, (n_orb,))
+    call("smx_project_bin", ctypes.byref(geo), _prec(dt), _ptr(bufs.samples), _ptr(bufs.n_stored), bufs.slots,
+         _ptr(bufs.info), _ptr(t_total), _ptr(bin_mapping), _ptr(num_per_bin), _ptr(v0), _ptr(s), _ptr(library),
+         _ptr(valid), _stream())
+    return library
+
+
+class Workspace:
+    """Grow-only device scratch shared by calls on one stream."""
+
+    def __init__(self):
+        self.buf = None
+
+    def get(self, nbytes, device):
+        if self.buf is None or self.buf.numel() < nbytes or self.buf.device != device:
+            self.buf = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
+        return self.buf
+
+
+_ws = Workspace()
+_ws_maps = Workspace()
+
+
+def nnls_admm(library, row_map, row_scale, Y, maxiter, lambda_reg, w_init, mixed):
+    """library (n, ld) float/double; row_map (m,) int32; row_scale (m,) double;
+    Y (B, m) double -> Z (B, n) double."""
+    n, ld = library.shape
+    m = row_map.numel()
+    B = Y.shape[0]
+    _check(library, "library", library.dtype, (n, ld))
+    _check(row_map, "row_map", torch.int32, (m,))
+    _check(row_scale, "row_scale", torch.float64, (m,))
+    _check(Y, "Y", torch.float64, (B, m))
+    prob = SmxNnlsProblem(n=n, m=m, n_rhs=B, ld_lib=ld, lib_precision=_prec(library.dtype),
+                          mode=_lib.SMX_NNLS_MIXED if mixed else _lib.SMX_NNLS_FP64, maxiter=int(maxiter),
+                          lambda_reg=float(lambda_reg), w_init=float(w_init))
+    nbytes = ctypes.c_size_t(0)
+    call("smx_nnls_workspace_size", ctypes.byref(prob), ctypes.byref(nbytes))
+    ws = _ws.get(nbytes.value, library.device)
+    Z = torch.empty(B, n, dtype=torch.float64, device=library.device)
+    call("smx_nnls_admm", ctypes.byref(prob), _ptr(library), _ptr(row_map), _ptr(row_scale), _ptr(Y), _ptr(Z),
+         _ptr(ws), ws.numel(), _stream())
+    return Z
+
+
+def model_maps(library, n_cells, n_bins, W, gamma_kin, v0, s, y_rz, y_xy, y_xy_boot, y_h_boot, sig_h_raw,
+               lum_factor, sigma_amplify=1.0, want_maps=True):
+    n, ld = library.shape
+    B = W.shape[0]
+    _check(W, "W", torch.float64, (B, n))
+    for t, nm, sh in ((gamma_kin, "gamma_kin", (n_bins,)), (v0, "v0", (n_bins,)), (s, "s", (n_bins,)),
+                      (y_rz, "y_rz", (n_cells,)), (y_xy, "y_xy", (n_bins,)), (y_xy_boot, "y_xy_boot", (B, n_bins)),
+                      (y_h_boot, "y_h_boot", (4, B, n_bins)), (sig_h_raw, "sig_h_raw", (4, n_bins))):
+        _check(t, nm, torch.float64, sh)
+    prob = SmxMapsProblem(n=n, n_rhs=B, ld_lib=ld, lib_precision=_prec(library.dtype), n_cells=n_cells,
+                          n_bins=n_bins, lum_factor=float(lum_factor), sigma_amplify=float(sigma_amplify))
+    nbytes = ctypes.c_size_t(0)
+    call("smx_model_maps_workspace_size", ctypes.byref(prob), ctypes.byref(nbytes))
+    ws = _ws_maps.get(nbytes.value, library.device)
+    maps = torch.empty(B, n_cells + 7 * n_bins, dtype=torch.float64, device=library.device) if want_maps else None
+    logl = torch.empty(B, dtype=torch.float64, device=library.device)
+    call("smx_model_maps", ctypes.byref(prob), _ptr(library), _ptr(W), _ptr(gamma_kin), _ptr(v0), _ptr(s),
+         _ptr(y_rz), _ptr(y_xy), _ptr(y_xy_boot), _ptr(y_h_boot), _ptr(sig_h_raw), _ptr(maps), _ptr(logl), _ptr(ws),
+         ws.numel(), _stream())
+    return maps, logl

@@ -1,0 +1,92 @@
+"""The canonical SchwarMAX potential and stellar density, as descriptors.
+
+The reference passes ``density_func`` and ``potential_func`` as Python
+callables into jitted code (likelihood.py:13-71).  Callables cannot cross a C
+ABI, so this package exposes the canonical pair as descriptor objects: they
+are recognised by ``build_model`` and friends, which then run the inline
+sm_103a kernels; calling them directly on CUDA tensors evaluates the model
+through ``smx_potential_eval``.  Any other callable is rejected with
+NotImplementedError.
+
+Model (likelihood.py:10-71): NFW halo (potentials.py:18-27) + Miyamoto-Nagai
+disc (potentials.py:29-65) + Dehnen-Aly T3 bar with gamma = 1
+(dehnen_bar.py:1318-1326, 1425-1438) + Dehnen-Aly V4 bulge with a = b = 0.5,
+L = 0.1, gamma = 0 (dehnen_bar.py:1371-1383, 1526-1543) whose mass is tied to
+the bar mass unless ``bulge_mass`` is given.
+"""
+import torch
+
+from . import kernels
+from ._lib import SmxPotential
+
+V4_A, V4_B, V4_L, V4_GAMMA = 0.5, 0.5, 0.1, 0.0
+GAMMA_BAR = 1.0
+
+
+def potential_struct(params_baryon, params_halo, bulge_mass=None):
+    """Reference parameter dicts -> smx_potential.  Shifted or tilted components
+    (potentials.py:8-15) are not part of the canonical model."""
+    for p in (params_baryon, params_halo):
+        for k in ("x_origin", "y_origin", "z_origin", "dirx", "diry"):
+            if k in p and float(p[k]) != 0.0:
+                raise NotImplementedError(f"non-canonical component geometry: {k}={float(p[k])}")
+        if "dirz" in p and float(p["dirz"]) <= 0.0:
+            raise NotImplementedError("the symmetry axis must be +z")
+    m_bar = 10.0 ** float(params_baryon["logM_bar"])
+    return SmxPotential(
+        halo_M=10.0 ** float(params_halo["logM"]), halo_Rs=float(params_halo["Rs"]),
+        halo_qa=float(params_halo.get("a", 1.0)), halo_qb=float(params_halo.get("b", 1.0)),
+        halo_qc=float(params_halo.get("c", 1.0)),
+        disc_M=10.0 ** float(params_baryon["logM_disc"]), disc_a=float(params_baryon["Rs_disc"]),
+        disc_b=float(params_baryon["Hs_disc"]),
+        bar_M=m_bar, bar_a=float(params_baryon["a_bar"]), bar_b=float(params_baryon["b_bar"]),
+        bar_L=float(params_baryon["L_bar"]), bar_gamma=GAMMA_BAR,
+        bulge_M=m_bar if bulge_mass is None else float(bulge_mass), bulge_a=V4_A, bulge_b=V4_B, bulge_L=V4_L,
+        bulge_gamma=V4_GAMMA)
+
+
+class _Canonical:
+    kind = None
+
+    def __repr__(self):
+        return f"<schwarmax_gb300 canonical {self.kind}>"
+
+
+class DensityFunc(_Canonical):
+    """density_func(x, y, z, params) -> rho, CUDA tensors in and out."""
+    kind = "density_func"
+
+    def __call__(self, x, y, z, params):
+        pot = potential_struct(params, dict(logM=0.0, Rs=1.0))
+        return kernels.potential_eval(pot, x, y, z, want_phi=False, want_acc=False, want_rho=True)["rho"]
+
+
+class PotentialFunc(_Canonical):
+    """potential_func(x, y, z, params_baryon, params_halo) -> Phi, CUDA tensors in and out."""
+    kind = "potential_func"
+
+    def __call__(self, x, y, z, params_baryon, params_halo):
+        pot = potential_struct(params_baryon, params_halo)
+        return kernels.potential_eval(pot, x, y, z, want_phi=True, want_acc=False)["phi"]
+
+    def acceleration(self, x, y, z, params_baryon, params_halo):
+        """-grad Phi (the reference's acc_fn, model.py:152-157) as a (3, n) tensor."""
+        pot = potential_struct(params_baryon, params_halo)
+        return kernels.potential_eval(pot, x, y, z, want_phi=False, want_acc=True)["acc"]
+
+
+density_func = DensityFunc()
+potential_func = PotentialFunc()
+
+
+def require_canonical(density, potential):
+    if density is not None and not isinstance(density, DensityFunc):
+        raise NotImplementedError("only the canonical density_func (MN + T3 + V4) has a GB300 kernel")
+    if potential is not None and not isinstance(potential, PotentialFunc):
+        raise NotImplementedError("only the canonical potential_func (NFW + MN + T3 + V4) has a GB300 kernel")
+
+
+def as_cuda(x, dtype):
+    if isinstance(x, torch.Tensor):
+        return x.to(device="cuda", dtype=dtype).contiguous()
+    return torch.as_tensor(x, dtype=dtype, device="cuda").contiguous()
