@@ -115,7 +115,7 @@ typedef struct {
                               variant does (integrates.py:319-512) */
     int n_attempts;        /* reference mode: N_max */
     int n_samples;         /* sampled mode */
-    int64_t max_attempts;  /* sampled mode: cap per orbit (status bit 2 when hit) */
+    int64_t max_attempts;  /* sampled mode: cap per orbit (status bit 1 when hit) */
     double atol, rtol, dt_min, dt_max;
     double omega;          /* frame angular velocity Omega = -Omega_bar (kpc/Gyr) */
 } smx_integrator;
@@ -174,6 +174,15 @@ int smx_project_bin(const smx_binning *geo, int precision, const void *samples,
                     const void *t_total, const int32_t *bin_mapping, const double *num_per_bin,
                     const double *v0, const double *s, void *library, int8_t *valid,
                     void *stream);
+
+/* Cells of individual points (fourfold images when geo->symmetry), with the
+ * same arithmetic as smx_project_bin; replaces the index part of bin_chunk
+ * (integrates.py:115-146) and assign_regular_grid (utils.py:10-42).
+ *   points SoA (6, n); cells, bins (n_img, n) int32 with n_img = 4 or 1
+ *   (cell = n_cells and bin = -1 mark points outside); vlos (n_img, n) km/s,
+ *   optional. */
+int smx_sample_cells(const smx_binning *geo, int precision, const void *points, int64_t n,
+                     const int32_t *bin_mapping, int32_t *cells, int32_t *bins, void *vlos, void *stream);
 
 /* ------------------------------------------------------------------- NNLS */
 enum { SMX_NNLS_FP64 = 0, SMX_NNLS_MIXED = 1 };

@@ -28,7 +28,7 @@ INFO_T, INFO_EJ0, INFO_EJ, INFO_WSUM, INFO_NACC, INFO_NATT, INFO_FIELDS = range(
 
 EXPORTS = ["smx_version", "smx_status_string", "smx_last_error", "smx_potential_eval",
            "smx_initial_conditions", "smx_density_target", "smx_integrate", "smx_project_bin",
-           "smx_nnls_workspace_size", "smx_nnls_admm", "smx_model_maps", "smx_model_maps_workspace_size"]
+           "smx_sample_cells", "smx_nnls_workspace_size", "smx_nnls_admm", "smx_model_maps", "smx_model_maps_workspace_size"]
 
 
 class SmxError(RuntimeError):
@@ -134,6 +134,7 @@ _SIGS = {
                        _I64, _P, _P, _P, _P, _P, _P], ctypes.c_int),
     "smx_project_bin": ([ctypes.POINTER(SmxBinning), ctypes.c_int, _P, _P, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _P],
                         ctypes.c_int),
+    "smx_sample_cells": ([ctypes.POINTER(SmxBinning), ctypes.c_int, _P, _I64, _P, _P, _P, _P, _P], ctypes.c_int),
     "smx_nnls_workspace_size": ([ctypes.POINTER(SmxNnlsProblem), ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
     "smx_nnls_admm": ([ctypes.POINTER(SmxNnlsProblem), _P, _P, _P, _P, _P, _P, ctypes.c_size_t, _P], ctypes.c_int),
     "smx_model_maps_workspace_size": ([ctypes.POINTER(SmxMapsProblem), ctypes.POINTER(ctypes.c_size_t)],

@@ -104,12 +104,22 @@ static int layout(const smx_nnls_problem *p, Layout *L, cusolverDnHandle_t solve
     return SMX_OK;
 }
 
+// U[i*m + r] = lib[i*ld + row_map[r]] * row_scale[r]; a row index outside
+// [0, ld) is not read: the entry is set to 0 and flag[0] records the error.
 template <typename TL, typename TU>
 __global__ void build_u_kernel(const TL *__restrict__ lib, int64_t ld, const int32_t *__restrict__ row_map,
-                               const double *__restrict__ row_scale, int64_t m, int64_t n, TU *U) {
-    const int64_t i = blockIdx.y;   // orbit
-    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < m; r += (int64_t)gridDim.x * blockDim.x)
-        U[i * m + r] = TU((double)lib[i * ld + row_map[r]] * row_scale[r]);
+                               const double *__restrict__ row_scale, int64_t m, int64_t n, TU *U, int *flag) {
+    for (int64_t i = blockIdx.y; i < n; i += gridDim.y) {
+        for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < m; r += (int64_t)gridDim.x * blockDim.x) {
+            const int64_t src = row_map[r];
+            if (src < 0 || src >= ld) {
+                flag[0] = 1;
+                U[i * m + r] = TU(0);
+            } else {
+                U[i * m + r] = TU((double)lib[i * ld + src] * row_scale[r]);
+            }
+        }
+    }
 }
 
 template <typename TU>
@@ -223,13 +233,13 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
     int *dinfo = (int *)(ws + L.info);
     double *V = (double *)(ws + L.V);
     SMX_TRY_CUDA(cudaMemsetAsync(frob, 0, sizeof(double), s));
-    SMX_TRY_CUDA(cudaMemsetAsync(dinfo, 0, sizeof(int), s));
-    dim3 gb((unsigned)((m + 255) / 256 < 65535 ? (m + 255) / 256 : 65535), (unsigned)n);
+    SMX_TRY_CUDA(cudaMemsetAsync(dinfo, 0, 4 * sizeof(int), s));
+    dim3 gb((unsigned)((m + 255) / 256 < 65535 ? (m + 255) / 256 : 65535), (unsigned)(n < 65535 ? n : 65535));
     const double one = 1.0, zero = 0.0;
     const float onef = 1.0f, zerof = 0.0f;
     if (!mixed) {
         double *U = (double *)(ws + L.U);
-        build_u_kernel<TL, double><<<gb, 256, 0, s>>>(lib, p->ld_lib, row_map, row_scale, m, n, U);
+        build_u_kernel<TL, double><<<gb, 256, 0, s>>>(lib, p->ld_lib, row_map, row_scale, m, n, U, dinfo + 3);
         frob_kernel<double><<<grid1d(m * n), 256, 0, s>>>(U, m * n, frob);
         SMX_TRY_BLAS(cublasSetMathMode(h->blas, CUBLAS_DEFAULT_MATH));
         SMX_TRY_BLAS(cublasDsyrk(h->blas, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, (int)m, (int)n, &one, U, (int)m, &zero,
@@ -257,7 +267,7 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
     } else {
         float *U = (float *)(ws + L.U);
         float *Gf = (float *)(ws + L.Gf);
-        build_u_kernel<TL, float><<<gb, 256, 0, s>>>(lib, p->ld_lib, row_map, row_scale, m, n, U);
+        build_u_kernel<TL, float><<<gb, 256, 0, s>>>(lib, p->ld_lib, row_map, row_scale, m, n, U, dinfo + 3);
         frob_kernel<float><<<grid1d(m * n), 256, 0, s>>>(U, m * n, frob);
         SMX_TRY_BLAS(cublasSetMathMode(h->blas, CUBLAS_TF32_TENSOR_OP_MATH));
         SMX_TRY_BLAS(cublasGemmEx(h->blas, CUBLAS_OP_N, CUBLAS_OP_T, (int)m, (int)m, (int)n, &onef, U, CUDA_R_32F,
@@ -307,9 +317,10 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
     }
     SMX_TRY_CUDA(cudaGetLastError());
     // the factorisation status is read back: a failed Cholesky is reported, not silently used
-    int hinfo[3] = {0, 0, 0};
+    int hinfo[4] = {0, 0, 0, 0};
     SMX_TRY_CUDA(cudaMemcpyAsync(hinfo, dinfo, sizeof(hinfo), cudaMemcpyDeviceToHost, s));
     SMX_TRY_CUDA(cudaStreamSynchronize(s));
+    if (hinfo[3] != 0) return set_error(SMX_ERR_ARGUMENT, "row_map holds an index outside [0, ld_lib)");
     if (hinfo[0] != 0) return set_error(SMX_ERR_NUMERIC, "Cholesky of rho' I + U U^T failed (info=%d)", hinfo[0]);
     return SMX_OK;
 }

@@ -58,6 +58,47 @@ __device__ __forceinline__ int grid_cell(const T (&v)[D], const T *lo, const T *
     return out ? oob : flat;
 }
 
+
+// Rzphi cell (n_cells = outside), Voronoi bin (-1 = outside) and line-of-sight
+// velocity of one phase-space point (integrates.py:120-146).
+template <typename T>
+__device__ __forceinline__ void project_image(const GeoT<T> &G, T x, T y, T z, T vx, T vy, T vz,
+                                              const int32_t *__restrict__ bin_mapping, int &cell, int &b, T &vl) {
+    const T R = RN<T>::sqrt(RN<T>::add(RN<T>::mul(x, x), RN<T>::mul(y, y)));
+    const T ph = M<T>::atan2(y, x);
+    const T cyl[3] = {R, z, ph};
+    cell = grid_cell<T, 3>(cyl, G.lo, G.span, G.fn, G.n, G.n_cells);
+    const T X = RN<T>::add(RN<T>::add(RN<T>::mul(G.rot[0], x), RN<T>::mul(G.rot[1], y)), RN<T>::mul(G.rot[2], z));
+    const T Y = RN<T>::add(RN<T>::add(RN<T>::mul(G.rot[3], x), RN<T>::mul(G.rot[4], y)), RN<T>::mul(G.rot[5], z));
+    const T sky[2] = {X, Y};
+    const int pix = grid_cell<T, 2>(sky, G.xlo, G.xspan, G.xfn, G.nx, G.n_pix);
+    b = __ldg(&bin_mapping[pix]);
+    vl = RN<T>::add(RN<T>::add(RN<T>::mul(G.rot[6], vx), RN<T>::mul(G.rot[7], vy)), RN<T>::mul(G.rot[8], vz));
+}
+
+// Per-sample cells of the fourfold images, for exactness checks and callers
+// that bin on their own: cells/bins (n_img, N) int32, vlos (n_img, N) km/s.
+template <typename T>
+__global__ void sample_cells_kernel(GeoT<T> G, const T *__restrict__ pts, int64_t N,
+                                    const int32_t *__restrict__ bin_mapping, int32_t *cells, int32_t *bins,
+                                    T *vlos) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const T q[6] = {pts[i], pts[N + i], pts[2 * N + i], pts[3 * N + i], pts[4 * N + i], pts[5 * N + i]};
+    const int n_img = G.symmetry ? 4 : 1;
+    for (int im = 0; im < n_img; ++im) {
+        const T sxy = (im >= 2) ? T(-1) : T(1);
+        const T sz = (im == 1 || im == 3) ? T(-1) : T(1);
+        int cell, b;
+        T vl;
+        project_image(G, sxy * q[0], sxy * q[1], sz * q[2], sxy * q[3], sxy * q[4], sz * q[5], bin_mapping, cell, b,
+                      vl);
+        cells[im * N + i] = cell;
+        bins[im * N + i] = b;
+        if (vlos) vlos[im * N + i] = vl * T(kKpcGyrToKms);
+    }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) project_bin_kernel(GeoT<T> G, const T *__restrict__ samples,
                                                          const int32_t *__restrict__ n_stored, int64_t slots,
@@ -126,18 +167,11 @@ __global__ void __launch_bounds__(256) project_bin_kernel(GeoT<T> G, const T *__
                 const T sz = (im == 1 || im == 3) ? T(-1) : T(1);
                 const T x = sxy * q[0], y = sxy * q[1], z = sz * q[2];
                 const T vx = sxy * q[3], vy = sxy * q[4], vz = sz * q[5];
-                const T R = RN<T>::sqrt(RN<T>::add(RN<T>::mul(x, x), RN<T>::mul(y, y)));
-                const T ph = M<T>::atan2(y, x);
-                const T cyl[3] = {R, z, ph};
-                const int cell = grid_cell<T, 3>(cyl, G.lo, G.span, G.fn, G.n, G.n_cells);
+                int cell, b;
+                T vl;
+                project_image(G, x, y, z, vx, vy, vz, bin_mapping, cell, b, vl);
                 if (cell < G.n_cells) atomicAdd(&acc[cell], w);
-                const T X = RN<T>::add(RN<T>::add(RN<T>::mul(G.rot[0], x), RN<T>::mul(G.rot[1], y)), RN<T>::mul(G.rot[2], z));
-                const T Y = RN<T>::add(RN<T>::add(RN<T>::mul(G.rot[3], x), RN<T>::mul(G.rot[4], y)), RN<T>::mul(G.rot[5], z));
-                const T sky[2] = {X, Y};
-                const int pix = grid_cell<T, 2>(sky, G.xlo, G.xspan, G.xfn, G.nx, G.n_pix);
-                const int b = __ldg(&bin_mapping[pix]);
                 if (b < 0 || b >= nb) continue;
-                const T vl = RN<T>::add(RN<T>::add(RN<T>::mul(G.rot[6], vx), RN<T>::mul(G.rot[7], vy)), RN<T>::mul(G.rot[8], vz));
                 const T s_b = T(__ldg(&sg[b]));
                 const T yv = (vl * kms - T(__ldg(&v0g[b]))) / s_b;
                 const T gw = w * isq2pi / s_b * M<T>::exp(T(-0.5) * yv * yv);
@@ -164,9 +198,7 @@ __global__ void __launch_bounds__(256) project_bin_kernel(GeoT<T> G, const T *__
 }
 
 template <typename T>
-static int launch(const smx_binning *g, const void *samples, const int32_t *n_stored, int64_t slots,
-                  const void *info, const void *t_total, const int32_t *bin_mapping, const double *num_per_bin,
-                  const double *v0, const double *s, void *library, int8_t *valid, cudaStream_t st) {
+static GeoT<T> make_geo(const smx_binning *g) {
     GeoT<T> G;
     const double lo[3] = {g->R_lo, g->z_lo, g->phi_lo}, hi[3] = {g->R_hi, g->z_hi, g->phi_hi};
     const int n[3] = {g->nR, g->nz, g->nphi};
@@ -192,6 +224,14 @@ static int launch(const smx_binning *g, const void *samples, const int32_t *n_st
     G.n_part = g->n_part;
     G.n_real = g->n_real;
     G.symmetry = g->symmetry;
+    return G;
+}
+
+template <typename T>
+static int launch(const smx_binning *g, const void *samples, const int32_t *n_stored, int64_t slots,
+                  const void *info, const void *t_total, const int32_t *bin_mapping, const double *num_per_bin,
+                  const double *v0, const double *s, void *library, int8_t *valid, cudaStream_t st) {
+    const GeoT<T> G = make_geo<T>(g);
     const size_t smem = (size_t)G.rows * sizeof(T);
     int dev = 0, max_smem = 0;
     SMX_TRY_CUDA(cudaGetDevice(&dev));
@@ -233,4 +273,27 @@ extern "C" int smx_project_bin(const smx_binning *geo, int precision, const void
         return launch<double>(geo, samples, n_stored, slots, info, t_total, bin_mapping, num_per_bin, v0, s, library,
                               valid, st);
     return set_error(SMX_ERR_ARGUMENT, "bad precision %d", precision);
+}
+
+extern "C" int smx_sample_cells(const smx_binning *geo, int precision, const void *points, int64_t n,
+                                const int32_t *bin_mapping, int32_t *cells, int32_t *bins, void *vlos,
+                                void *stream) {
+    if (!geo) return set_error(SMX_ERR_ARGUMENT, "smx_sample_cells: geometry is NULL");
+    if (n < 0 || geo->nR < 1 || geo->nz < 1 || geo->nphi < 1 || geo->nX < 1 || geo->nY < 1)
+        return set_error(SMX_ERR_ARGUMENT, "smx_sample_cells: bad sizes");
+    if (n == 0) return SMX_OK;
+    if (!points || !bin_mapping || !cells || !bins) return set_error(SMX_ERR_ARGUMENT, "smx_sample_cells: NULL buffer");
+    cudaStream_t st = (cudaStream_t)stream;
+    const unsigned grid = (unsigned)((n + 255) / 256);
+    if (precision == SMX_FP32) {
+        sample_cells_kernel<float><<<grid, 256, 0, st>>>(make_geo<float>(geo), (const float *)points, n, bin_mapping,
+                                                         cells, bins, (float *)vlos);
+    } else if (precision == SMX_FP64) {
+        sample_cells_kernel<double><<<grid, 256, 0, st>>>(make_geo<double>(geo), (const double *)points, n,
+                                                          bin_mapping, cells, bins, (double *)vlos);
+    } else {
+        return set_error(SMX_ERR_ARGUMENT, "bad precision %d", precision);
+    }
+    SMX_TRY_CUDA(cudaGetLastError());
+    return SMX_OK;
 }

@@ -201,3 +201,18 @@ def model_maps(library, n_cells, n_bins, W, gamma_kin, v0, s, y_rz, y_xy, y_xy_b
          _ptr(y_rz), _ptr(y_xy), _ptr(y_xy_boot), _ptr(y_h_boot), _ptr(sig_h_raw), _ptr(maps), _ptr(logl), _ptr(ws),
          ws.numel(), _stream())
     return maps, logl
+
+
+def sample_cells(geo: SmxBinning, points, bin_mapping):
+    """points (6, N) -> (cells (n_img, N), bins (n_img, N), vlos (n_img, N) km/s)."""
+    dt = points.dtype
+    N = points.shape[1]
+    _check(points, "points", dt, (6, N))
+    _check(bin_mapping, "bin_mapping", torch.int32, (geo.nX * geo.nY + 1,))
+    n_img = 4 if geo.symmetry else 1
+    cells = torch.empty(n_img, N, dtype=torch.int32, device=points.device)
+    bins = torch.empty(n_img, N, dtype=torch.int32, device=points.device)
+    vlos = torch.empty(n_img, N, dtype=dt, device=points.device)
+    call("smx_sample_cells", ctypes.byref(geo), _prec(dt), _ptr(points), N, _ptr(bin_mapping), _ptr(cells),
+         _ptr(bins), _ptr(vlos), _stream())
+    return cells, bins, vlos

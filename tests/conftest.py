@@ -37,3 +37,13 @@ def gpu_available():
         return torch.cuda.is_available()
     except Exception:
         return False
+
+
+def tiny_dict_data(g):
+    """dict_data of the end_to_end golden case, with the reference's draws."""
+    dd = {k[3:]: g[k] for k in g if k.startswith("dd_")}
+    dd["total_bins"] = int(dd["total_bins"])
+    dd["Rzphi_n_tot"] = int(dd["Rzphi_n_tot"])
+    dd["jeans_normals"] = g["jeans_normals"]
+    dd["jitter_uniforms"] = g["jitter_uniforms"]
+    return dd

@@ -1,0 +1,85 @@
+"""End-to-end GPU evaluations through the reference-named entry points,
+against golden vectors produced by the reference's own code."""
+import numpy as np
+import pytest
+
+from conftest import golden, tiny_dict_data
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def smx():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import schwarmax_gb300
+    return schwarmax_gb300
+
+
+def _grid_kw(dd):
+    return dict(Rzphi_n_grid=dd["Rzphi_n_grid"], Rzphi_lim_grid=np.array([dd["R_minmax"], dd["z_minmax"],
+                                                                          dd["phi_minmax"]]),
+                xy_lim_grid=np.array([dd["X_minmax"], dd["Y_minmax"]]), xy_n_grid=dd["nX_nY"])
+
+
+def test_model_likelihood_fp64_matches_reference(smx):
+    g = golden("end_to_end")
+    dd = tiny_dict_data(g)
+    logl = smx.model_likelihood(g["theta"], dd, 4, 48, sigma_amplify=float(g["sigma_amplify"]),
+                                settings=dict(precision="fp64"))
+    ref = float(g["logL"])
+    assert abs(logl - ref) <= 1e-6 * abs(ref), (logl, ref)
+
+
+def test_build_model_fp64_matches_reference(smx):
+    g = golden("end_to_end")
+    dd = tiny_dict_data(g)
+    halo, bary = smx.unpack_params(g["theta"])
+    out = smx.build_model(smx.density_func, smx.potential_func, halo, bary, dd, 4, 48, nnls_maxiter=60,
+                          settings=dict(precision="fp64"), **_grid_kw(dd))
+    for k in ("density_3d", "density_3d_model", "surface_density", "h1", "h2", "h3", "h4", "V", "sigma", "weights"):
+        ref = g["bm_" + k]
+        np.testing.assert_allclose(out[k].cpu().numpy(), ref, rtol=0, atol=1e-5 * np.abs(ref).max(), err_msg=k)
+
+
+def test_model_likelihood_mixed_precision_error(smx):
+    """FP32 orbits + mixed NNLS against the reference's FP64 logL on the tiny case."""
+    g = golden("end_to_end")
+    dd = tiny_dict_data(g)
+    logl = smx.model_likelihood(g["theta"], dd, 4, 48, sigma_amplify=float(g["sigma_amplify"]))
+    ref = float(g["logL"])
+    assert np.isfinite(logl)
+    assert abs(logl - ref) <= 0.02 * abs(ref), (logl, ref)
+
+
+def test_calculate_delta_chi2_fp64_matches_reference(smx):
+    g = golden("end_to_end")
+    dd = tiny_dict_data(g)
+    d = smx.calculate_delta_chi2(g["theta"], dd, 4, 48, settings=dict(precision="fp64"))
+    ref = float(g["delta_chi2"])
+    assert abs(d - ref) <= 1e-5 * abs(ref), (d, ref)
+
+
+def test_get_model_with_orbit_fp64_matches_reference(smx):
+    g = golden("end_to_end")
+    w = golden("with_orbit")
+    dd = tiny_dict_data(g)
+    dd["jitter_uniforms_traj"] = w["jitter_uniforms"]
+    halo, bary = smx.unpack_params(g["theta"])
+    out = smx.get_model_with_orbit(smx.density_func, smx.potential_func, halo, bary, dd, 4, 48, nnls_maxiter=60,
+                                   settings=dict(precision="fp64"), **_grid_kw(dd))
+    for k in ("t_traj", "y_traj", "weights_all_boot", "density_3d_model", "surface_density", "h1", "V", "sigma"):
+        ref = w["mo_" + k]
+        np.testing.assert_allclose(out[k].cpu().numpy(), ref, rtol=0, atol=1e-5 * np.abs(ref).max(), err_msg=k)
+
+
+def test_noncanonical_model_rejected(smx):
+    g = golden("end_to_end")
+    dd = tiny_dict_data(g)
+    halo, bary = smx.unpack_params(g["theta"])
+    with pytest.raises(NotImplementedError):
+        smx.build_model(lambda *a: 0, smx.potential_func, halo, bary, dd, 4, 48, **_grid_kw(dd))
+    bad = dict(bary, x_origin=1.0)
+    with pytest.raises(NotImplementedError):
+        smx.build_model(smx.density_func, smx.potential_func, halo, bad, dd, 4, 48, **_grid_kw(dd))
