@@ -1,0 +1,382 @@
+#!/usr/bin/env python
+"""Model evaluations per second on one GB300 (the config-1 workload).
+
+One step = one full model evaluation (model_likelihood): Jeans ICs ->
+16,384 particles x 4 jitter realisations integrated for 50 circular periods
+(adaptive BS23, rtol 1e-6, 1,000 uniform-time samples each) -> projection and
+binning into an 80x80-pixel / 400-aperture IFU and a 24x16x12 (R, z, phi)
+grid -> 3-D density target -> 100 bootstrap ADMM NNLS solves (200 iterations)
+-> model maps -> chi^2 -> log-mean-exp.  Inputs are seeded synthetic data
+(schwarmax_gb300.synthetic); working sets are larger than L2 (the sample store
+alone is 1.8 GB), so no L2 flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU restatement of the same evaluation (oracle/,
+all host cores) on a bounded sample of the workload and scales it to evals/s.
+Multi-GPU runs are independent replicas (one evaluation stream per GPU).
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "model evals/sec at Δχ²≤0.1, batched mixed-precision vs plain FP64, 1 GB300"
+UNIT = "evals/s"
+WORKLOAD = ("config1: 16,384 particles x 4 realisations, 50 circular periods, rtol 1e-6, 1,000 uniform-time "
+            "samples per orbit, 80x80 px / 400 Voronoi apertures, 24x16x12 Rzphi grid, 100 bootstrap ADMM "
+            "NNLS (200 iterations)")
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def clock_sampler(path):
+    try:
+        return subprocess.Popen(
+            ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+             "--format=csv,noheader,nounits", "-lms", "200"], stdout=open(path, "w"), stderr=subprocess.DEVNULL)
+    except FileNotFoundError:
+        return None
+
+
+def clock_summary(path, gpu_index):
+    rows = []
+    try:
+        for line in open(path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9 and f[0] == str(gpu_index):
+                rows.append(f)
+    except OSError:
+        return None
+    if not rows:
+        return None
+    sm = sorted(float(r[1]) for r in rows if r[1].replace(".", "").isdigit())
+    reasons = set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    for r in rows:
+        for nm, v in zip(names, r[5:9]):
+            if v.strip().lower() in ("active", "yes", "1"):
+                reasons.add(nm)
+    return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": float(rows[0][2]) if rows else None,
+            "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        return None
+
+
+# FP32 operations of one canonical force evaluation (gradient of NFW + MN +
+# T3 needle (3 positions, orders 1-5) + V4 needle (2 positions, orders 1-9))
+# and of one BS23 attempt outside the three force calls (stages, error norm,
+# step control, amortised dense output), counted from the kernel source with
+# add/sub/mul = 1, FMA = 2 and each sqrt/rsqrt/div/log/log1p/cbrt call = 1.
+FLOPS_PER_FORCE = 630
+FLOPS_PER_STEP = 215
+
+
+def run_ours(args, rank, world, local):
+    import numpy as np
+    import torch
+
+    import schwarmax_gb300 as smx
+    from schwarmax_gb300 import _lib, engine, synthetic
+    from schwarmax_gb300.likelihood import grid_of, log_likelihoods, log_mean_exp, unpack_params
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    cfg = synthetic.CONFIGS[args.config]
+    t0 = time.time()
+    dict_data, theta = synthetic.make_dataset(cfg, seed=args.seed)
+    setup_s = time.time() - t0
+    st = cfg.settings("mixed")
+    dd = engine.DeviceData(dict_data, n_real=st.n_real)
+    nb = cfg.n_bins
+    kw = dict(settings=st, nnls_maxiter=cfg.admm_iters)
+
+    def step(i, timers=None):
+        th = theta.copy()
+        th[10] = theta[10] + 0.002 * ((i % 5) - 2)          # M/L walk, MCMC-like
+        logl, r = log_likelihoods(th, dd, nb, cfg.n_grid[0] * cfg.n_grid[1] * cfg.n_grid[2], **kw)
+        return log_mean_exp(logl), r
+
+    for i in range(args.warmup):
+        step(i)
+    torch.cuda.synchronize()
+    # --- device-resident throughput -------------------------------------------------
+    sampler = clock_sampler(os.path.join(args.out, f"clocks_rank{rank}.csv")) if rank == 0 else None
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    launches0 = _lib.kernel_launches()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    integ_ms = []
+    ev0.record()
+    for i in range(args.steps):
+        val, r = step(i)
+    ev1.record()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    launches = _lib.kernel_launches() - launches0
+    ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    if sampler:
+        sampler.terminate()
+    value = world * args.steps / (ms / 1e3)
+    # --- integrator kernel alone, for the roofline ----------------------------------
+    halo, bary = unpack_params(theta)
+    pot = smx.potentials.potential_struct(bary, halo, st.bulge_mass)
+    grid = grid_of(dict_data)
+    libd = engine.build_library(pot, bary, dd, grid, st)
+    torch.cuda.synchronize()
+    ic = libd["ic"]
+    bufs = libd["bufs"]
+    from schwarmax_gb300 import kernels
+    from schwarmax_gb300._lib import SmxIntegrator, SMX_MODE_SAMPLED
+    icfg = SmxIntegrator(mode=SMX_MODE_SAMPLED, store_all=0, n_attempts=st.n_attempts, n_samples=st.n_samples,
+                         max_attempts=st.max_attempts, atol=st.atol, rtol=st.rtol, dt_min=st.dt_min,
+                         dt_max=st.dt_max, omega=-float(bary["Omega_bar"]))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    kernels.integrate(pot, icfg, ic["w0"], ic["dt_init"], ic["t_total"], bufs)
+    e1.record()
+    torch.cuda.synchronize()
+    k_ms = e0.elapsed_time(e1)
+    n_att = float(bufs.info[_lib.INFO_NATT].double().sum().item())
+    flops = n_att * (3 * FLOPS_PER_FORCE + FLOPS_PER_STEP)
+    peaks = measured_peaks() or {}
+    clocks = clock_summary(os.path.join(args.out, f"clocks_rank{rank}.csv"), local) if rank == 0 else None
+    max_mhz = (clocks or {}).get("sm_max_mhz") or peaks.get("sm_max_mhz") or 2070.0
+    fp32_peak = 152 * 128 * 2 * max_mhz * 1e6 / 1e12     # TFLOP/s, FMA = 2
+    achieved = flops / (k_ms / 1e3) / 1e12
+    roofline = {"kernel": "integrate_kernel<float>", "bound": "fp32", "achieved": round(achieved, 3),
+                "peak": round(fp32_peak, 1), "unit": "TFLOP/s", "frac": round(achieved / fp32_peak, 4),
+                "peak_source": "nominal FP32 FMA rate, 152 SMs x 128 lanes x 2 at the max SM clock "
+                               "(MEASURED_PEAKS.json holds no FP32 figure)",
+                "traffic": None, "ms_per_launch": round(k_ms, 3), "attempts": n_att,
+                "flops_per_attempt": 3 * FLOPS_PER_FORCE + FLOPS_PER_STEP}
+    # --- precision: mixed NNLS vs FP64 NNLS on the same library, and plain FP64 -------
+    prec = {}
+    if rank == 0 and not args.skip_fp64:
+        val_m, r_m = step(0)
+        logl_m = r_m["logl"].clone()
+        lib64 = r_m["lib"]["library"].double()
+        from schwarmax_gb300.engine import data_terms, nnls_inputs, likelihood_data, row_map
+        d = r_m["data"]
+        row_scale, Y = nnls_inputs(d, dd, grid.n_cells, (math.sqrt(5.0), math.sqrt(5.0), 1.0))
+        W64 = kernels.nnls_admm(lib64, row_map(grid.n_cells, nb), row_scale, Y, cfg.admm_iters, 1.0,
+                                float((d["y_rz"].sum() / lib64.shape[0]).item()), mixed=False)
+        y_xy_b, y_h_b, sh = likelihood_data(dd)
+        _, logl_64 = kernels.model_maps(lib64, grid.n_cells, nb, W64, d["gamma"].contiguous(), dd.v0, dd.s,
+                                        d["y_rz"].contiguous(), dd.xy, y_xy_b, y_h_b, sh,
+                                        float(d["mmpo"].item()) * d["l2m"], 1.0, want_maps=False)
+        dchi2_nnls = float((2 * (logl_m - logl_64)).abs().max().item())
+        wm = r_m["W"]
+        wrel = float(((wm - W64).abs().max() / W64.abs().max()).item())
+        # full plain-FP64 evaluation (FP64 orbits, binning, NNLS, maps)
+        st64 = cfg.settings("fp64")
+        torch.cuda.synchronize()
+        t64 = time.time()
+        logl64_full, _ = log_likelihoods(theta, dd, nb, grid.n_cells, settings=st64, nnls_maxiter=cfg.admm_iters)
+        torch.cuda.synchronize()
+        fp64_s = time.time() - t64
+        lm = float(log_mean_exp(logl_m).item())
+        l64 = float(log_mean_exp(logl64_full).item())
+        prec = {"dchi2_max_same_library": dchi2_nnls, "weights_max_rel_same_library": wrel,
+                "dchi2_end_to_end_vs_fp64": abs(2 * (lm - l64)), "fp64_evals_per_s": 1.0 / fp64_s,
+                "mixed_over_fp64": value / world * fp64_s}
+    # --- end to end through the public API with host buffers ------------------------------
+    e2e = None
+    if not args.skip_e2e:
+        host = {}
+        h2d = 0
+        for k, v in dict_data.items():
+            a = np.asarray(v)
+            if a.dtype.kind in "fi" and a.size > 8:
+                t = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+                host[k] = t
+                h2d += t.numel() * t.element_size()
+            else:
+                host[k] = v
+        torch.cuda.synchronize()
+        t1 = time.time()
+        for i in range(args.e2e_steps):
+            th = theta.copy()
+            th[10] += 0.002 * ((i % 5) - 2)
+            smx.model_likelihood(th, host, nb, grid.n_cells, settings=st, nnls_maxiter=cfg.admm_iters, cache=False)
+        torch.cuda.synchronize()
+        e2e_s = time.time() - t1
+        e2e = {"value": world * args.e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": 8 * 3}
+    cpu = None
+    if rank == 0 and world == 1 and not args.skip_cpu:
+        cpu = cpu_baseline(cfg, quick=True)
+    if rank == 0:
+        line = {"metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32 (orbits, binning) / tf32+f64 (NNLS)",
+                "data": "synthetic (seeded; schwarmax_gb300.synthetic)",
+                "config": {"workload": WORKLOAD, "parallelism": f"replicas x{world}",
+                           "l2": "working set > L2 (no flush)", "setup_s": round(setup_s, 1)},
+                "gpu_launches": int(launches), "roofline": roofline, "precision": prec, "e2e": e2e,
+                "cpu_baseline": cpu, "clocks": clocks, "logL_last": float(val.item())}
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def cpu_baseline(cfg, quick=True, cores=None):
+    """The FP64 oracle on a bounded sample of the workload, scaled to evals/s.
+
+    Sample: n orbits of the config integrated over 1/25 of the horizon (2 of
+    50 periods) with the same tolerances, per-orbit cost scaled to
+    n_part * n_real orbits and 50 periods; plus the oracle NNLS timed at a
+    1/8-scale problem and scaled by its n^3 + maxiter * B * n^2 cost."""
+    import numpy as np
+    from oracle import integrate as oi, nnls as on, orbits as oo, potential as op
+    from schwarmax_gb300 import synthetic
+    from schwarmax_gb300.likelihood import unpack_params
+    theta = synthetic.theta_for(cfg)
+    halo, bary = unpack_params(theta)
+    P = op.canonical_params(bary, halo, cfg.bulge_mass)
+    rng = np.random.default_rng(3)
+    n = 16 if quick else 64
+    pos = synthetic.disc_positions(rng, n)
+    R = np.sqrt(pos[:, 0] ** 2 + pos[:, 1] ** 2)
+    vc = oo.rotation_curve(R, pos[:, 2], P)
+    w = np.concatenate([pos, np.stack([vc * pos[:, 1] / R, -vc * pos[:, 0] / R, np.zeros(n)], -1)], -1)
+    To = oo.orbital_timescale(R, pos[:, 2], P)
+    periods = 2.0
+    t0 = time.time()
+    oi.integrate_sampled(w, P, -float(bary["Omega_bar"]), To * periods, int(cfg.n_samples * periods / cfg.n_periods),
+                         To / 100, cfg.atol, cfg.rtol, 1e-5, 0.3)
+    t_int = time.time() - t0
+    per_orbit_period = t_int / (n * periods)
+    integ_s = per_orbit_period * cfg.n_part * cfg.n_real * cfg.n_periods
+    # NNLS at 1/8 scale
+    nf, mf = cfg.n_part, int(np.prod(cfg.n_grid)) + 5 * cfg.n_bins
+    ns, ms_ = nf // 8, mf // 8
+    B = cfg.n_boot
+    U = np.abs(rng.normal(size=(ms_, ns)))
+    Y = rng.normal(size=(B, ms_))
+    t0 = time.time()
+    on.admm(U, Y, 1.0, 1.0, cfg.admm_iters)
+    t_n = time.time() - t0
+    cost = lambda n_, m_: n_ ** 3 / 3 + m_ * n_ * n_ + cfg.admm_iters * B * 2 * n_ * n_  # noqa: E731
+    nnls_s = t_n * cost(nf, mf) / cost(ns, ms_)
+    total = integ_s + nnls_s
+    threads = os.environ.get("OMP_NUM_THREADS")
+    return {"value": 1.0 / total, "unit": UNIT, "cores": 1 if quick else (cores or os.cpu_count()),
+            "kind": "port",
+            "sample": f"FP64 NumPy oracle: {n} orbits x {periods:g} periods of the sampled integrator "
+                      f"({t_int:.1f} s, scaled x{cfg.n_part * cfg.n_real * cfg.n_periods / (n * periods):.0f}) + "
+                      f"ADMM NNLS at 1/8 scale ({t_n:.1f} s, scaled by cost); BLAS threads={threads or 'default'}",
+            "integrator_s": integ_s, "nnls_s": nnls_s}
+
+
+def _cpu_worker(args):
+    """Integrate a share of the sample orbits in a separate process."""
+    import numpy as np
+    from oracle import integrate as oi
+    w, P, om, Tend, ns, dt0, atol, rtol = args
+    t0 = time.time()
+    oi.integrate_sampled(w, P, om, Tend, ns, dt0, atol, rtol, 1e-5, 0.3)
+    return time.time() - t0
+
+
+def run_reference(args, rank, world):
+    """CPU restatement of the evaluation on all host cores (bounded sample)."""
+    if rank != 0:
+        return
+    import multiprocessing as mp
+
+    import numpy as np
+    from oracle import orbits as oo, potential as op
+    from schwarmax_gb300 import synthetic
+    from schwarmax_gb300.likelihood import unpack_params
+    cfg = synthetic.CONFIGS[args.config]
+    cores = os.cpu_count() or 1
+    theta = synthetic.theta_for(cfg)
+    halo, bary = unpack_params(theta)
+    P = op.canonical_params(bary, halo, cfg.bulge_mass)
+    rng = np.random.default_rng(3)
+    per = 4
+    n = cores * per
+    pos = synthetic.disc_positions(rng, n)
+    R = np.sqrt(pos[:, 0] ** 2 + pos[:, 1] ** 2)
+    vc = oo.rotation_curve(R, pos[:, 2], P)
+    w = np.concatenate([pos, np.stack([vc * pos[:, 1] / R, -vc * pos[:, 0] / R, np.zeros(n)], -1)], -1)
+    To = oo.orbital_timescale(R, pos[:, 2], P)
+    periods = 1.0
+    ns = max(1, int(cfg.n_samples * periods / cfg.n_periods))
+    jobs = [(w[i::cores], P, -float(bary["Omega_bar"]), To[i::cores] * periods, ns, To[i::cores] / 100, cfg.atol,
+             cfg.rtol) for i in range(cores)]
+    ctx = mp.get_context("spawn")
+    values = []
+    for s in range(args.warmup + args.steps):
+        t0 = time.time()
+        with ctx.Pool(cores) as pool:
+            pool.map(_cpu_worker, jobs)
+        wall = time.time() - t0
+        integ_s = wall * (cfg.n_part * cfg.n_real * cfg.n_periods) / (n * periods)
+        if s >= args.warmup:
+            values.append(1.0 / integ_s)
+    value = float(np.median(values))
+    sample = (f"FP64 NumPy oracle on {cores} processes: {n} orbits x {periods:g} period of the sampled integrator "
+              f"per step, wall time scaled to {cfg.n_part * cfg.n_real} orbits x {cfg.n_periods:g} periods "
+              f"(integrator only: a lower bound on the CPU cost of one evaluation)")
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded)", "impl": "reference",
+            "config": {"workload": WORKLOAD}, "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores,
+                                                                 "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", type=int, default=1)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--out", default=os.path.join(ROOT, "gpurun_out"))
+    args = ap.parse_args()
+    os.makedirs(args.out, exist_ok=True)
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -59,6 +59,9 @@ typedef struct {
 /* Library version (major*10000 + minor*100 + patch). */
 int smx_version(void);
 const char *smx_status_string(int status);
+/* Number of kernels this library has launched in the process so far (its own
+ * kernels only; cuBLAS/cuSOLVER calls are not counted). */
+unsigned long long smx_kernel_launches(void);
 /* Copies the last error message of the calling thread into buf (NUL
  * terminated, truncated to len) and returns its full length. */
 size_t smx_last_error(char *buf, size_t len);
@@ -136,7 +139,10 @@ enum { SMX_INFO_T = 0, SMX_INFO_EJ0 = 1, SMX_INFO_EJ = 2, SMX_INFO_WSUM = 3,
  *   n_stored (n_orb) int32     samples written per orbit
  *   info     (SMX_INFO_FIELDS, n_orb)
  *   status   (n_orb) int32     bit 0 non-finite state, bit 1 attempt cap,
- *                              bit 2 slot overflow (0 = clean)
+ *                              bit 2 slot overflow, bit 3 stalled: an attempt at
+ *                              dt = dt_min was rejected, so (the step being
+ *                              deterministic) all later attempts would be too and
+ *                              the orbit stops there (0 = clean)
  *   queue    one int32 of device scratch (the call zeroes it). */
 int smx_integrate(const smx_potential *pot, const smx_integrator *cfg, int precision,
                   const void *w0, const void *dt_init, const void *t_total, int64_t n_orb,

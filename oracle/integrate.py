@@ -15,7 +15,9 @@ Two sampling modes share the stepper:
   "sampled":   integrate until t >= T_end and emit S samples at the midpoints
       t_j = (j + 1/2) T_end / S of S equal intervals, interpolated with the
       cubic Hermite dense output of each accepted step (y, y3, k1, k4), each
-      with weight T_end / S.  Attempts are capped at max_attempts.
+      with weight T_end / S.  Attempts are capped at max_attempts.  An orbit whose
+      attempt at dt = dt_min is rejected stalls (every later attempt would repeat
+      it) and keeps only the samples emitted so far.
 
 Binning of samples with the fourfold bar symmetry, GH accumulation,
 normalisation by T_integrated = 4 sum(weights) + EPSILON, the E_J / time
@@ -106,6 +108,7 @@ def integrate_sampled(w0, P, Om, T_end, n_samples, dt_init, atol, rtol, dt_min, 
     n_acc = np.zeros(N, dtype=np.int64)
     n_att = np.zeros(N, dtype=np.int64)
     active = np.ones(N, dtype=bool)
+    stalled = np.zeros(N, dtype=bool)
     h = T_end / n_samples
     while active.any():
         idx = np.nonzero(active)[0]
@@ -132,11 +135,14 @@ def integrate_sampled(w0, P, Om, T_end, n_samples, dt_init, atol, rtol, dt_min, 
             k1[a] = f1
             t[a] = t1
             n_acc[a] += 1
+        # a rejection at dt_min repeats forever (same state and step): the orbit stalls
+        stalled[idx[~acc & (dt[idx] <= dt_min)]] = True
         dt[idx] = dt_new
-        active = (nxt < n_samples) & (n_att < max_attempts)
+        active = (nxt < n_samples) & (n_att < max_attempts) & ~stalled
     capped = nxt < n_samples
     return dict(ys=ys, weight=T_end / n_samples, t_final=t, y_final=y, EJ0=EJ0,
-                EJ_final=orbits.jacobi_energy(y, P, Om), n_acc=n_acc, n_att=n_att, capped=capped)
+                EJ_final=orbits.jacobi_energy(y, P, Om), n_acc=n_acc, n_att=n_att, capped=capped,
+                stalled=stalled, n_emitted=nxt)
 
 
 class BinGeometry:
@@ -261,7 +267,9 @@ def library_from_states(w0_batch, T_total, dt_init, P, Omega_bar, geo, mode="ref
     elif mode == "sampled":
         res = integrate_sampled(w0, P, Om, T_total, n_samples, dt_init, atol, rtol, dt_min, dt_max,
                                 max_attempts=max_attempts)
-        acc.add(res["ys"], np.broadcast_to(res["weight"][None, :], res["ys"].shape[:2]))
+        j = np.arange(n_samples)[:, None]
+        wts = np.where(j < res["n_emitted"][None, :], res["weight"][None, :], 0.0)
+        acc.add(res["ys"], wts)
     else:
         raise ValueError(mode)
     Rz, surf, h, valid = normalise(acc, res["EJ0"], res["EJ_final"], res["t_final"], T_total)

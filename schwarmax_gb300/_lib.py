@@ -26,7 +26,7 @@ SMX_MODE_REFERENCE, SMX_MODE_SAMPLED = 0, 1
 SMX_NNLS_FP64, SMX_NNLS_MIXED = 0, 1
 INFO_T, INFO_EJ0, INFO_EJ, INFO_WSUM, INFO_NACC, INFO_NATT, INFO_FIELDS = range(7)
 
-EXPORTS = ["smx_version", "smx_status_string", "smx_last_error", "smx_potential_eval",
+EXPORTS = ["smx_version", "smx_kernel_launches", "smx_status_string", "smx_last_error", "smx_potential_eval",
            "smx_initial_conditions", "smx_density_target", "smx_integrate", "smx_project_bin",
            "smx_sample_cells", "smx_nnls_workspace_size", "smx_nnls_admm", "smx_model_maps", "smx_model_maps_workspace_size"]
 
@@ -122,6 +122,7 @@ _P = ctypes.c_void_p
 _I64 = ctypes.c_int64
 _SIGS = {
     "smx_version": ([], ctypes.c_int),
+    "smx_kernel_launches": ([], ctypes.c_ulonglong),
     "smx_status_string": ([ctypes.c_int], ctypes.c_char_p),
     "smx_last_error": ([ctypes.c_char_p, ctypes.c_size_t], ctypes.c_size_t),
     "smx_potential_eval": ([ctypes.POINTER(SmxPotential), ctypes.c_int, _P, _P, _P, _I64, _P, _P, _P, _P, _P, _P],
@@ -170,6 +171,11 @@ def last_error():
     buf = ctypes.create_string_buffer(2048)
     lib.smx_last_error(buf, 2048)
     return buf.value.decode(errors="replace")
+
+
+def kernel_launches():
+    """Kernels launched so far by this process through the library."""
+    return int(load().smx_kernel_launches())
 
 
 def call(name, *args):

@@ -3,6 +3,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <atomic>
 #include <string>
 
 #include "smx_internal.cuh"
@@ -10,6 +11,9 @@
 namespace smx {
 
 static thread_local std::string g_last_error;
+static std::atomic<unsigned long long> g_launches{0};
+
+void count_launch(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 int set_error(int status, const char *fmt, ...) {
     char buf[1024];
@@ -50,6 +54,8 @@ int validate_potential(const smx_potential *p) {
 extern "C" {
 
 int smx_version(void) { return 100; }
+
+unsigned long long smx_kernel_launches(void) { return smx::g_launches.load(std::memory_order_relaxed); }
 
 const char *smx_status_string(int s) {
     switch (s) {

@@ -137,11 +137,26 @@ __global__ void __launch_bounds__(128) integrate_kernel(PotT<T> P, IntegT<T> I, 
                     wsum += dt;
                 }
                 t = t1;
-            } else if (!sampled && I.store_all) {
-                const int64_t slot = att - 1;
-                if (slot < slots) put(samples, n_orb, slots, orb, slot, y, T(0));
-                else flags |= 4;
-                stored = slot + 1;
+            } else {
+                if (!sampled && I.store_all) {
+                    const int64_t slot = att - 1;
+                    if (slot < slots) put(samples, n_orb, slots, orb, slot, y, T(0));
+                    else flags |= 4;
+                    stored = slot + 1;
+                }
+                if (dt <= I.dt_min) {
+                    // Rejected at the smallest step: the next attempt repeats this one
+                    // exactly (same y, k1 and dt = dt_min), so every later attempt is
+                    // rejected too.  Stop here; a trajectory store gets the remaining
+                    // attempts as the same zero-weight state.
+                    flags |= 8;
+                    if (!sampled && I.store_all) {
+                        for (int64_t slot = att; slot < att_cap && slot < slots; ++slot)
+                            put(samples, n_orb, slots, orb, slot, y, T(0));
+                        stored = att_cap < slots ? att_cap : slots;
+                    }
+                    break;
+                }
             }
             T sf = T(0.9) * M<T>::rcbrt(en > T(1e-10) ? en : T(1e-10));
             sf = sf < T(0.2) ? T(0.2) : (sf > T(5) ? T(5) : sf);
@@ -190,6 +205,7 @@ static int launch(const smx_potential *pot, const smx_integrator *cfg, const voi
     integrate_kernel<T><<<(unsigned)blocks, 128, 0, s>>>(make_pot<T>(*pot), I, (const T *)w0, (const T *)dt_init,
                                                          (const T *)t_total, n_orb, slots, (T *)samples, n_stored,
                                                          (T *)info, status, queue);
+    count_launch();
     SMX_TRY_CUDA(cudaGetLastError());
     return SMX_OK;
 }

@@ -170,6 +170,7 @@ extern "C" int smx_model_maps(const smx_maps_problem *p, const void *library, co
         float *Mp = (float *)(ws + L.Mp);
         const int64_t cnt = n * B;
         d2f_kernel<<<(unsigned)((cnt + 255) / 256 < 4864 ? (cnt + 255) / 256 : 4864), 256, 0, st>>>(W, Wf, cnt);
+        count_launch();
         const float one = 1.f, zero = 0.f;
         cublasStatus_t bs = cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, rows, (int)B, (int)n, &one, (const float *)library,
                                         (int)p->ld_lib, Wf, (int)n, &zero, Mp, rows);
@@ -177,6 +178,7 @@ extern "C" int smx_model_maps(const smx_maps_problem *p, const void *library, co
         maps_chi2_kernel<float><<<(unsigned)B, 256, 0, st>>>(Mp, rows, p->n_cells, p->n_bins, gamma_kin, v0, s, y_rz,
                                                             y_xy, y_xy_boot, y_h_boot, sig_h_raw, B, p->lum_factor,
                                                             p->sigma_amplify, maps_out, part);
+        count_launch();
     } else if (p->lib_precision == SMX_FP64) {
         double *Mp = (double *)(ws + L.Mp);
         const double one = 1.0, zero = 0.0;
@@ -186,10 +188,12 @@ extern "C" int smx_model_maps(const smx_maps_problem *p, const void *library, co
         maps_chi2_kernel<double><<<(unsigned)B, 256, 0, st>>>(Mp, rows, p->n_cells, p->n_bins, gamma_kin, v0, s, y_rz,
                                                              y_xy, y_xy_boot, y_h_boot, sig_h_raw, B, p->lum_factor,
                                                              p->sigma_amplify, maps_out, part);
+        count_launch();
     } else {
         return set_error(SMX_ERR_ARGUMENT, "bad library precision %d", p->lib_precision);
     }
     logl_kernel<<<1, 128, 0, st>>>(part, B, logl_out);
+    count_launch();
     SMX_TRY_CUDA(cudaGetLastError());
     return SMX_OK;
 }

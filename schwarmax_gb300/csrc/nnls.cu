@@ -240,11 +240,14 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
     if (!mixed) {
         double *U = (double *)(ws + L.U);
         build_u_kernel<TL, double><<<gb, 256, 0, s>>>(lib, p->ld_lib, row_map, row_scale, m, n, U, dinfo + 3);
+        count_launch();
         frob_kernel<double><<<grid1d(m * n), 256, 0, s>>>(U, m * n, frob);
+        count_launch();
         SMX_TRY_BLAS(cublasSetMathMode(h->blas, CUBLAS_DEFAULT_MATH));
         SMX_TRY_BLAS(cublasDsyrk(h->blas, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, (int)m, (int)n, &one, U, (int)m, &zero,
                                  G, (int)m));
         add_diag_kernel<<<grid1d(m), 256, 0, s>>>(G, m, frob, lam, (double)n);
+        count_launch();
         SMX_TRY_SOLVER(cusolverDnDpotrf(h->solver, CUBLAS_FILL_MODE_LOWER, (int)m, G, (int)m, (double *)(ws + L.work),
                                         L.lwork, dinfo));
         SMX_TRY_CUDA(cudaMemcpyAsync(V, Y, sizeof(double) * m * B, cudaMemcpyDeviceToDevice, s));
@@ -254,6 +257,7 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
         SMX_TRY_BLAS(cublasDgemm(h->blas, CUBLAS_OP_T, CUBLAS_OP_N, (int)n, (int)B, (int)m, &one, U, (int)m, V, (int)m,
                                  &zero, Wc, (int)n));
         admm_init_kernel<double><<<grid1d(n * B), 256, 0, s>>>(Z, Uu, D, n * B, p->w_init);
+        count_launch();
         for (int it = 0; it < p->maxiter; ++it) {
             SMX_TRY_BLAS(cublasDgemm(h->blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)m, (int)B, (int)n, &one, U, (int)m, D,
                                      (int)n, &zero, E, (int)m));
@@ -262,18 +266,22 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
             SMX_TRY_BLAS(cublasDgemm(h->blas, CUBLAS_OP_T, CUBLAS_OP_N, (int)n, (int)B, (int)m, &one, U, (int)m, E,
                                      (int)m, &zero, Gt, (int)n));
             admm_update_kernel<double><<<grid1d(n * B), 256, 0, s>>>(Gt, Wc, Z, Uu, D, n * B, frob, lam, (double)n);
+            count_launch();
         }
         SMX_TRY_CUDA(cudaMemcpyAsync(Z_out, Z, sizeof(double) * n * B, cudaMemcpyDeviceToDevice, s));
     } else {
         float *U = (float *)(ws + L.U);
         float *Gf = (float *)(ws + L.Gf);
         build_u_kernel<TL, float><<<gb, 256, 0, s>>>(lib, p->ld_lib, row_map, row_scale, m, n, U, dinfo + 3);
+        count_launch();
         frob_kernel<float><<<grid1d(m * n), 256, 0, s>>>(U, m * n, frob);
+        count_launch();
         SMX_TRY_BLAS(cublasSetMathMode(h->blas, CUBLAS_TF32_TENSOR_OP_MATH));
         SMX_TRY_BLAS(cublasGemmEx(h->blas, CUBLAS_OP_N, CUBLAS_OP_T, (int)m, (int)m, (int)n, &onef, U, CUDA_R_32F,
                                   (int)m, U, CUDA_R_32F, (int)m, &zerof, Gf, CUDA_R_32F, (int)m,
                                   CUBLAS_COMPUTE_32F_FAST_TF32, CUBLAS_GEMM_DEFAULT));
         shift_gram_kernel<float><<<grid1d(m * m), 256, 0, s>>>(Gf, G, m, frob, lam, (double)n);
+        count_launch();
         SMX_TRY_SOLVER(cusolverDnDpotrf(h->solver, CUBLAS_FILL_MODE_LOWER, (int)m, G, (int)m, (double *)(ws + L.work),
                                         L.lwork, dinfo));
         // V = G^-1 Y in double (one-off), Wc = U^T V in float
@@ -281,6 +289,7 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
         SMX_TRY_SOLVER(cusolverDnDpotrs(h->solver, CUBLAS_FILL_MODE_LOWER, (int)m, (int)B, G, (int)m, V, (int)m, dinfo + 1));
         float *Vf = (float *)(ws + L.Vf);
         convert_kernel<float><<<grid1d(m * B), 256, 0, s>>>(V, Vf, m * B);
+        count_launch();
         float *Wc = (float *)(ws + L.Wc), *Z = (float *)(ws + L.Z), *Uu = (float *)(ws + L.Uu),
               *D = (float *)(ws + L.D), *E = (float *)(ws + L.E), *F = (float *)(ws + L.F), *Gt = (float *)(ws + L.Gt);
         SMX_TRY_BLAS(cublasSetMathMode(h->blas, CUBLAS_DEFAULT_MATH));
@@ -291,14 +300,17 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
         // matrices once the factor has been copied out.
         float *Lf = Gf;
         tril_to_float_kernel<<<grid1d(m * m), 256, 0, s>>>(G, Lf, m);
+        count_launch();
         float *Linv = (float *)G;
         float *Gi = (float *)G + m * m;
         identity_kernel<<<grid1d(m * m), 256, 0, s>>>(Linv, m);
+        count_launch();
         SMX_TRY_BLAS(cublasStrsm(h->blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT,
                                  (int)m, (int)m, &onef, Lf, (int)m, Linv, (int)m));
         SMX_TRY_BLAS(cublasSgemm(h->blas, CUBLAS_OP_T, CUBLAS_OP_N, (int)m, (int)m, (int)m, &onef, Linv, (int)m, Linv,
                                  (int)m, &zerof, Gi, (int)m));
         admm_init_kernel<float><<<grid1d(n * B), 256, 0, s>>>(Z, Uu, D, n * B, p->w_init);
+        count_launch();
         SMX_TRY_BLAS(cublasSetMathMode(h->blas, CUBLAS_TF32_TENSOR_OP_MATH));
         for (int it = 0; it < p->maxiter; ++it) {
             SMX_TRY_BLAS(cublasGemmEx(h->blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)m, (int)B, (int)n, &onef, U, CUDA_R_32F,
@@ -311,9 +323,11 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
                                       (int)m, F, CUDA_R_32F, (int)m, &zerof, Gt, CUDA_R_32F, (int)n,
                                       CUBLAS_COMPUTE_32F_FAST_TF32, CUBLAS_GEMM_DEFAULT));
             admm_update_kernel<float><<<grid1d(n * B), 256, 0, s>>>(Gt, Wc, Z, Uu, D, n * B, frob, lam, (double)n);
+            count_launch();
         }
         SMX_TRY_BLAS(cublasSetMathMode(h->blas, CUBLAS_DEFAULT_MATH));
         f2d_kernel<<<grid1d(n * B), 256, 0, s>>>(Z, Z_out, n * B);
+        count_launch();
     }
     SMX_TRY_CUDA(cudaGetLastError());
     // the factorisation status is read back: a failed Cholesky is reported, not silently used

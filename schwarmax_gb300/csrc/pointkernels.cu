@@ -159,10 +159,12 @@ int smx_potential_eval(const smx_potential *pot, int precision, const void *x, c
     if (precision == SMX_FP32) {
         potential_eval_kernel<float><<<blocks_for(n, bs), bs, 0, s>>>(make_pot<float>(*pot), (const float *)x,
             (const float *)y, (const float *)z, n, (float *)phi, (float *)ax, (float *)ay, (float *)az, (float *)rho);
+        count_launch();
     } else if (precision == SMX_FP64) {
         potential_eval_kernel<double><<<blocks_for(n, bs), bs, 0, s>>>(make_pot<double>(*pot), (const double *)x,
             (const double *)y, (const double *)z, n, (double *)phi, (double *)ax, (double *)ay, (double *)az,
             (double *)rho);
+        count_launch();
     } else {
         return set_error(SMX_ERR_ARGUMENT, "bad precision %d", precision);
     }
@@ -188,10 +190,12 @@ int smx_initial_conditions(const smx_potential *pot, int precision, const void *
         initial_conditions_kernel<float><<<grid, bs, 0, s>>>(make_pot<float>(*pot), (const float *)pos,
             (const float *)normals, (const float *)uniforms, n, n_real, (float)n_periods, (float)steps_per_period,
             (float *)w_out, (float *)t_total, (float *)dt_init, (float *)w0_new, (float *)t_orb, (float *)vc);
+        count_launch();
     } else if (precision == SMX_FP64) {
         initial_conditions_kernel<double><<<grid, bs, 0, s>>>(make_pot<double>(*pot), (const double *)pos,
             (const double *)normals, (const double *)uniforms, n, n_real, n_periods, steps_per_period,
             (double *)w_out, (double *)t_total, (double *)dt_init, (double *)w0_new, (double *)t_orb, (double *)vc);
+        count_launch();
     } else {
         return set_error(SMX_ERR_ARGUMENT, "bad precision %d", precision);
     }
@@ -214,9 +218,11 @@ int smx_density_target(const smx_potential *pot, int precision, const double *R_
     if (precision == SMX_FP32) {
         density_target_kernel<float><<<grid, bs, 0, s>>>(make_pot<float>(*pot), R_grid, z_grid, phi_grid, n_cells,
                                                          dR, dz, dphi, sample, n_sample, (float *)out);
+        count_launch();
     } else if (precision == SMX_FP64) {
         density_target_kernel<double><<<grid, bs, 0, s>>>(make_pot<double>(*pot), R_grid, z_grid, phi_grid,
                                                           n_cells, dR, dz, dphi, sample, n_sample, (double *)out);
+        count_launch();
     } else {
         return set_error(SMX_ERR_ARGUMENT, "bad precision %d", precision);
     }

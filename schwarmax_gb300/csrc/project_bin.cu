@@ -243,6 +243,7 @@ static int launch(const smx_binning *g, const void *samples, const int32_t *n_st
     project_bin_kernel<T><<<g->n_part, 256, smem, st>>>(G, (const T *)samples, n_stored, slots, (const T *)info,
                                                         (const T *)t_total, bin_mapping, num_per_bin, v0, s, area,
                                                         (T *)library, valid);
+    count_launch();
     SMX_TRY_CUDA(cudaGetLastError());
     return SMX_OK;
 }
@@ -288,9 +289,11 @@ extern "C" int smx_sample_cells(const smx_binning *geo, int precision, const voi
     if (precision == SMX_FP32) {
         sample_cells_kernel<float><<<grid, 256, 0, st>>>(make_geo<float>(geo), (const float *)points, n, bin_mapping,
                                                          cells, bins, (float *)vlos);
+        count_launch();
     } else if (precision == SMX_FP64) {
         sample_cells_kernel<double><<<grid, 256, 0, st>>>(make_geo<double>(geo), (const double *)points, n,
                                                           bin_mapping, cells, bins, (double *)vlos);
+        count_launch();
     } else {
         return set_error(SMX_ERR_ARGUMENT, "bad precision %d", precision);
     }

@@ -24,6 +24,8 @@ constexpr double kEps = 1e-12;                         // EPSILON of constants.p
 constexpr double kPi = 3.14159265358979323846;
 
 int set_error(int status, const char *fmt, ...);
+// Process-wide count of kernels this library has launched (smx_kernel_launches).
+void count_launch(unsigned n = 1);
 int check_cuda(cudaError_t e, const char *what);
 void clear_error();
 

@@ -56,7 +56,7 @@ def test_potential_force_density_fp64(K, scale, bulge):
     np.testing.assert_allclose(out["phi"].cpu().numpy(), phi, rtol=1e-12)
     a = np.stack([ax, ay, az])
     amax = np.abs(a).max(0)
-    np.testing.assert_allclose(out["acc"].cpu().numpy() / amax, a / amax, rtol=0, atol=1e-11)
+    np.testing.assert_allclose(out["acc"].cpu().numpy() / amax, a / amax, rtol=0, atol=2e-10)
     np.testing.assert_allclose(out["rho"].cpu().numpy(), opot.rho(x, y, z, P), rtol=1e-10)
 
 
@@ -232,6 +232,8 @@ def test_integrate_trajectory_store_all_fp64(K):
 
 
 def test_integrate_sampled_fp64_matches_oracle(K):
+    """Uniform-time samples of the dense output; includes orbits that plunge to the
+    centre and stall at dt_min (status bit 3) and keep the samples emitted so far."""
     rng = np.random.default_rng(15)
     pb, ph = _params()
     S, P = _structs(pb, ph)
@@ -242,11 +244,16 @@ def test_integrate_sampled_fp64_matches_oracle(K):
     bufs = K.IntegratorBuffers(n, Sn, torch.float64, torch.device("cuda"))
     K.integrate(S, _integ_cfg(1, n_samples=Sn, omega=om, rtol=1e-6), _cuda(w.T, torch.float64),
                 _cuda(To / 100, torch.float64), _cuda(T_end, torch.float64), bufs)
-    ref = ointeg.integrate_sampled(w, P, om, T_end, Sn, To / 100, 1e-7, 1e-6, 1e-5, 0.3)
+    ref = ointeg.integrate_sampled(w, P, om, T_end, Sn, To / 100, 1e-7, 1e-6, 1e-5, 0.3, max_attempts=200000)
     smp = bufs.samples.cpu().numpy()
-    assert (bufs.n_stored.cpu().numpy() == Sn).all()
-    np.testing.assert_allclose(smp[:6].transpose(2, 1, 0), ref["ys"], rtol=1e-7, atol=1e-8)
-    np.testing.assert_allclose(smp[6], (T_end / Sn)[:, None] * np.ones((1, Sn)), rtol=1e-14)
+    nst = bufs.n_stored.cpu().numpy()
+    np.testing.assert_array_equal(nst, ref["n_emitted"])
+    st = bufs.status.cpu().numpy()
+    np.testing.assert_array_equal((st & 8) != 0, ref["stalled"])
+    assert ref["stalled"].any() and not ref["stalled"].all()
+    for o in range(n):
+        np.testing.assert_allclose(smp[:6, o, :nst[o]].T, ref["ys"][:nst[o], o], rtol=1e-7, atol=1e-8)
+        np.testing.assert_allclose(smp[6, o, :nst[o]], T_end[o] / Sn, rtol=1e-14)
     info = bufs.info.cpu().numpy()
     np.testing.assert_array_equal(info[4].astype(int), ref["n_acc"])
     np.testing.assert_array_equal(info[5].astype(int), ref["n_att"])
