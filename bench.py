@@ -145,6 +145,8 @@ def run_ours(args, rank, world, local):
     if sampler:
         sampler.terminate()
     value = world * args.steps / (ms / 1e3)
+    # --- per-stage device time of one evaluation (outside the timed region) ---------
+    stages = stage_breakdown(lambda: step(0))
     # --- integrator kernel alone, for the roofline ----------------------------------
     halo, bary = unpack_params(theta)
     pot = smx.potentials.potential_struct(bary, halo, st.bulge_mass)
@@ -240,11 +242,48 @@ def run_ours(args, rank, world, local):
                 "data": "synthetic (seeded; schwarmax_gb300.synthetic)",
                 "config": {"workload": WORKLOAD, "parallelism": f"replicas x{world}",
                            "l2": "working set > L2 (no flush)", "setup_s": round(setup_s, 1)},
-                "gpu_launches": int(launches), "roofline": roofline, "precision": prec, "e2e": e2e,
+                "gpu_launches": int(launches), "roofline": roofline, "stages_ms": stages, "precision": prec, "e2e": e2e,
                 "cpu_baseline": cpu, "clocks": clocks, "logL_last": float(val.item())}
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def stage_breakdown(fn):
+    """CUDA-event time of each library stage during one call of fn()."""
+    import torch
+
+    from schwarmax_gb300 import kernels
+    names = ["initial_conditions", "integrate", "project_bin", "density_target", "nnls_admm", "model_maps"]
+    events = {n: [] for n in names}
+    orig = {n: getattr(kernels, n) for n in names}
+
+    def wrap(n):
+        def f(*a, **k):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            r = orig[n](*a, **k)
+            e1.record()
+            events[n].append((e0, e1))
+            return r
+        return f
+
+    for n in names:
+        setattr(kernels, n, wrap(n))
+    try:
+        torch.cuda.synchronize()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record()
+        fn()
+        t1.record()
+        torch.cuda.synchronize()
+    finally:
+        for n in names:
+            setattr(kernels, n, orig[n])
+    out = {n: round(sum(a.elapsed_time(b) for a, b in events[n]), 3) for n in names}
+    out["total"] = round(t0.elapsed_time(t1), 3)
+    return out
 
 
 def cpu_baseline(cfg, quick=True, cores=None):

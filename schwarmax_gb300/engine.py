@@ -78,19 +78,21 @@ class DeviceData:
         self.source = d
 
         def dev(x, dtype=torch.float64):
+            if isinstance(x, torch.Tensor):    # host tensors (pinned when the caller pinned them)
+                return x.to(device, non_blocking=True).to(dtype).contiguous()
             a = torch.as_tensor(_np(x, np.float64 if dtype == torch.float64 else np.int32))
             if pin:
                 a = a.pin_memory()
             return a.to(device, dtype=dtype, non_blocking=pin).contiguous()
 
-        w0 = _np(d["w0"])
-        self.n = w0.shape[0]
+        w0 = d["w0"]
+        self.n = int(w0.shape[0])
         if "jeans_normals" in d and "jitter_uniforms" in d:
-            normals, uniforms = _np(d["jeans_normals"]), _np(d["jitter_uniforms"])
+            normals, uniforms = d["jeans_normals"], d["jitter_uniforms"]
         else:
             normals, uniforms = default_draws(self.n, max(n_real, 1))
         self.uniforms_traj = _np(d["jitter_uniforms_traj"]) if "jitter_uniforms_traj" in d else None
-        self.pos64 = dev(w0.T.copy())
+        self.pos64 = dev(w0).t().contiguous()
         self.normals64 = dev(normals)
         self.uniforms64 = dev(uniforms)
         self.bin_mapping = dev(d["bin_mapping"], torch.int32)

@@ -37,6 +37,9 @@ def unpack_params(params):
 
 
 def grid_of(dict_data):
+    if isinstance(dict_data, engine.DeviceData):
+        dict_data = dict_data.source
+
     def f(v):
         return [float(x) for x in (v.tolist() if hasattr(v, "tolist") else v)]
     nR = [int(v) for v in (dict_data["Rzphi_n_grid"].tolist() if hasattr(dict_data["Rzphi_n_grid"], "tolist")
