@@ -401,7 +401,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", type=int, default=1)
+    ap.add_argument("--config", default="1", help="1 (the benchmark), 0, 4 or 'small' (profiler captures)")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--skip-fp64", action="store_true")
@@ -409,6 +409,7 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--out", default=os.path.join(ROOT, "gpurun_out"))
     args = ap.parse_args()
+    args.config = int(args.config) if args.config.isdigit() else args.config
     os.makedirs(args.out, exist_ok=True)
     rank, world, local = dist_env()
     if args.impl == "reference":

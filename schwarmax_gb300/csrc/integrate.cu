@@ -91,7 +91,7 @@ __global__ void __launch_bounds__(128) integrate_kernel(PotT<T> P, IntegT<T> I, 
                 const T err = dt * (e1 * k1[c] + e2 * k2[c] + e3 * k3[c] + e4 * k4[c]);
                 const T ay = M<T>::abs(y[c]), ayn = M<T>::abs(yn[c]);
                 const T sc = I.atol + I.rtol * (ay > ayn ? ay : ayn);
-                const T q = err / sc;
+                const T q = err * M<T>::rcp(sc);
                 s += q * q;
             }
             const T en = M<T>::sqrt(s / T(6));
@@ -104,11 +104,12 @@ __global__ void __launch_bounds__(128) integrate_kernel(PotT<T> P, IntegT<T> I, 
                 ++n_acc;
                 const T t1 = t + dt;
                 if (sampled) {
+                    const T idt = M<T>::rcp(dt);
                     // emit all sample times (j + 1/2) h inside (t, t1] by cubic Hermite
                     while (next < I.n_samples) {
                         const T tj = (T(next) + T(0.5)) * h;
                         if (tj > t1) break;
-                        const T th = (tj - t) / dt;
+                        const T th = (tj - t) * idt;
                         const T th2 = th * th, th3 = th2 * th;
                         const T h00 = T(2) * th3 - T(3) * th2 + T(1);
                         const T h10 = (th3 - T(2) * th2 + th) * dt;

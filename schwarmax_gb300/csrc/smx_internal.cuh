@@ -46,6 +46,7 @@ template <> struct M<float> {
     static __device__ __forceinline__ float exp(float x) { return expf(x); }
     static __device__ __forceinline__ float atan2(float y, float x) { return atan2f(y, x); }
     static __device__ __forceinline__ float abs(float x) { return fabsf(x); }
+    static __device__ __forceinline__ float rcp(float x) { return __frcp_rn(x); }
 };
 template <> struct M<double> {
     static __device__ __forceinline__ double rsqrt(double x) { return ::rsqrt(x); }
@@ -56,6 +57,7 @@ template <> struct M<double> {
     static __device__ __forceinline__ double exp(double x) { return ::exp(x); }
     static __device__ __forceinline__ double atan2(double y, double x) { return ::atan2(y, x); }
     static __device__ __forceinline__ double abs(double x) { return ::fabs(x); }
+    static __device__ __forceinline__ double rcp(double x) { return 1.0 / x; }
 };
 
 // -------------------------------------------------------- potential params
@@ -108,13 +110,15 @@ template <typename T, bool GRAD> struct Rec {
         Ax = ir;
         if (GRAD) {
             // d A_1 / d u2 = 1/(2 r (xp + r)); (xp + r) = u2/(r - xp) for xp < 0
-            Au = (xp >= T(0)) ? T(0.5) * ir / (xp + r) : T(0.5) * ir * (r - xp) * iu2;
+            // one reciprocal for both branches: 1/(xp + r) = (r - xp)/u2 when xp < 0
+            const T q = (xp >= T(0)) ? M<T>::rcp(xp + r) : (r - xp) * iu2;
+            Au = T(0.5) * ir * q;
             Bu = T(0.5) * ir;
             Axu = T(-0.5) * ir * iR2;
         }
     }
     __device__ __forceinline__ T log_A1(T u2) const {
-        return (xp >= T(0)) ? M<T>::log(xp + r) : M<T>::log(u2 / (r - xp));
+        return M<T>::log((xp >= T(0)) ? xp + r : u2 * M<T>::rcp(r - xp));
     }
     // advance n -> n + 2
     __device__ __forceinline__ void step(int n, T iu2) {
@@ -143,7 +147,7 @@ template <typename T, bool GRAD> struct Rec {
 template <typename T, int K, int FIRST, bool GRAD>
 __device__ __forceinline__ void needle_sum(T x, T u2, T L, T c1, T c2, const T (&kc)[K],
                                            const T (&dkc)[K], T &S0, T &Sx, T &Su, T &SZ) {
-    const T iu2 = T(1) / u2;
+    const T iu2 = M<T>::rcp(u2);
     S0 = Sx = Su = SZ = T(0);
     if (c1 != T(0)) {
         Rec<T, GRAD> p, m;
@@ -156,7 +160,7 @@ __device__ __forceinline__ void needle_sum(T x, T u2, T L, T c1, T c2, const T (
                 if (k == 0) {
                     const T ax = M<T>::abs(x);
                     const T D = (x >= T(0)) ? (m.xp + m.r) : (p.r - p.xp);
-                    F = c1 * M<T>::log1p(T(2) * L * (T(1) + T(2) * ax / (p.r + m.r)) / D);
+                    F = c1 * M<T>::log1p(T(2) * L * (T(1) + T(2) * ax * M<T>::rcp(p.r + m.r)) * M<T>::rcp(D));
                 } else {
                     F = c1 * (p.A - m.A);
                 }
@@ -219,10 +223,10 @@ __device__ __forceinline__ void potential(const PotT<T> &P, T x, T y, T z, T &ph
         const T r = s2 * ir;
         const T q = r * P.iRs;
         const T l = M<T>::log1p(q);
-        const T ire = T(1) / (r + eps);
+        const T ire = M<T>::rcp(r + eps);
         if (WANT_PHI) phi += -P.GMh * l * ire;
         if (WANT_GRAD) {
-            const T dpdr = -P.GMh * (P.iRs / (T(1) + q) - l * ire) * ire;
+            const T dpdr = -P.GMh * (P.iRs * M<T>::rcp(T(1) + q) - l * ire) * ire;
             const T c = dpdr * ir;
             gx += c * x * P.iqa2;
             gy += c * y * P.iqb2;
@@ -239,7 +243,7 @@ __device__ __forceinline__ void potential(const PotT<T> &P, T x, T y, T z, T &ph
             const T c = P.GMd * iD * iD * iD;
             gx += c * rx;
             gy += c * ry;
-            gz += c * s * rz / zeta;
+            gz += c * s * rz * M<T>::rcp(zeta);
         }
     }
     {   // T3 bar (dehnen_bar.py:1318-1326)
@@ -256,7 +260,7 @@ __device__ __forceinline__ void potential(const PotT<T> &P, T x, T y, T z, T &ph
         if (WANT_GRAD) {
             gx += -G * Sx;
             gy += -G * Su * T(2) * y;
-            gz += -G * (SZ + Su * T(2) * Z) * (z / ze);
+            gz += -G * (SZ + Su * T(2) * Z) * (z * M<T>::rcp(ze));
         }
     }
     {   // V4 bulge (dehnen_bar.py:1371-1383)
@@ -266,7 +270,7 @@ __device__ __forceinline__ void potential(const PotT<T> &P, T x, T y, T z, T &ph
         const T u2 = y * y + Z * Z;
         const T h = T(0.5) * P.ub2;
         const T aZ = a * Z;
-        const T iz = T(1) / ze;
+        const T iz = M<T>::rcp(ze);
         const T kc[5] = {T(1), a * (Z - T(0.4) * a) + h,
                          T(3) * a * (T(0.2) * aZ * (Z + Z - a) + h * (Z - T(0.2) * a)),
                          aZ * aZ * (aZ + T(6) * h), T(7) * h * aZ * aZ * aZ * Z * iz};
@@ -279,7 +283,7 @@ __device__ __forceinline__ void potential(const PotT<T> &P, T x, T y, T z, T &ph
         if (WANT_GRAD) {
             gx += -G * Sx;
             gy += -G * Su * T(2) * y;
-            gz += -G * (SZ + Su * T(2) * Z) * (z / ze);
+            gz += -G * (SZ + Su * T(2) * Z) * (z * iz);
         }
     }
 }

@@ -54,6 +54,9 @@ CONFIGS = {
     0: Config("config0", 2048, 500, 40, 120, (20, 16, 10), 100),
     1: Config("config1", 16384, 1000, 80, 400, (24, 16, 12), 100),
     4: Config("config4", 65536, 1000, 120, 1500, (32, 32, 16), 200, bar_mass=2e10, omega_kms_kpc=40.0),
+    # config 1 over one circular period with 20 samples: the same orbit count and
+    # per-attempt work on a short horizon, for profiler captures
+    "small": Config("small", 16384, 20, 80, 400, (24, 16, 12), 100, n_periods=1.0),
 }
 
 
