@@ -4,7 +4,8 @@
 // One thread owns one orbit at a time, with the state, the FSAL derivative and
 // the step size in registers and the canonical forces evaluated inline.  Orbits
 // are handed out by a device counter, so in the sampled mode (uneven step
-// counts) a lane that finishes early takes the next orbit instead of idling.
+// counts) a lane that finishes early takes the next orbit instead of idling,
+// without leaving the loop the rest of its warp is in.
 // Samples are written orbit-major, (7, n_orb, slots), so the projection kernel
 // reads each orbit contiguously; consecutive writes of one thread land in the
 // same sectors and merge in L2.
@@ -46,6 +47,36 @@ __device__ __forceinline__ void put(T *samples, int64_t n_orb, int64_t slots, in
     base[6 * cs] = w;
 }
 
+// k1 = f(y0) and E_J0 of every orbit, computed once before the main loop so
+// that the loop never evaluates forces outside its attempt body.  k1 is parked
+// in slot 0 of the orbit's sample store until the orbit is picked up (its
+// first stored sample overwrites it later); E_J0 goes to its final place.
+template <typename T>
+__global__ void __launch_bounds__(128) integrate_init_kernel(PotT<T> P, T om, const T *__restrict__ w0,
+                                                            int64_t n_orb, int64_t slots, T *samples, T *info) {
+    const int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (o >= n_orb) return;
+    T y[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) y[c] = w0[c * n_orb + o];
+    T phi, gx, gy, gz;
+    potential<T, true, true>(P, y[0], y[1], y[2], phi, gx, gy, gz);
+    const T f[6] = {y[3] + om * y[1], y[4] - om * y[0], y[5], -gx + om * y[4], -gy - om * y[3], -gz};
+    const T ek = T(0.5) * (y[3] * y[3] + y[4] * y[4] + y[5] * y[5]);
+    info[SMX_INFO_EJ0 * n_orb + o] = ek + phi - om * (y[0] * y[4] - y[1] * y[3]);
+    T *base = samples + o * slots;
+    const int64_t cs = n_orb * slots;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) base[c * cs] = f[c];
+}
+
+// Main loop.  Every iteration is one BS23 attempt for every active lane: the
+// three stage evaluations run through one inlined force evaluation inside a
+// stage loop whose index is uniform across the warp, so the expensive part of
+// the body is convergent even though lanes hold different orbits at different
+// times.  A lane whose orbit ends (attempt cap, all samples emitted, stall or
+// non-finite state) writes its record and loads the next orbit from the queue
+// in the same iteration.
 template <typename T>
 __global__ void __launch_bounds__(128) integrate_kernel(PotT<T> P, IntegT<T> I, const T *__restrict__ w0,
                                                        const T *__restrict__ dt0, const T *__restrict__ t_end,
@@ -55,58 +86,77 @@ __global__ void __launch_bounds__(128) integrate_kernel(PotT<T> P, IntegT<T> I, 
     const T e1 = T(-5.0 / 72.0), e2 = T(1.0 / 12.0), e3 = T(1.0 / 9.0), e4 = T(-1.0 / 8.0);
     const T b1 = T(2.0 / 9.0), b2 = T(1.0 / 3.0), b3 = T(4.0 / 9.0);
     const T om = I.om;
-    for (;;) {
-        const int64_t orb = atomicAdd(queue, 1);
-        if (orb >= n_orb) break;
-        T y[6], k1[6], k2[6], k3[6], yn[6], yt[6];
+    const bool sampled = I.mode == SMX_MODE_SAMPLED;
+    const int att_cap = sampled ? (int)(I.max_attempts < 0x7fffffffLL ? I.max_attempts : 0x7fffffffLL) : I.n_attempts;
+    const int n_samp = I.n_samples;
+    const int islots = (int)(slots < 0x7fffffffLL ? slots : 0x7fffffffLL);
+    const int64_t cs = n_orb * slots;
+    T y[6], k1[6], k2[6], k3[6], k4[6], yn[6];
 #pragma unroll
-        for (int c = 0; c < 6; ++c) y[c] = w0[c * n_orb + orb];
-        T dt = dt0[orb];
-        T t = T(0);
-        rhs(P, om, y, k1);
-        const T EJ0 = jacobi(P, om, y);
-        int flags = 0;
-        int64_t n_acc = 0, att = 0, stored = 0;
-        T wsum = T(0);
-        const bool sampled = I.mode == SMX_MODE_SAMPLED;
-        const T Tend = sampled ? t_end[orb] : T(0);
-        const T h = sampled ? Tend / T(I.n_samples) : T(0);
-        int64_t next = 0;
-        const int64_t att_cap = sampled ? I.max_attempts : (int64_t)I.n_attempts;
-        while (att < att_cap && (!sampled || next < I.n_samples)) {
-            ++att;
+    for (int c = 0; c < 6; ++c) k2[c] = k3[c] = k4[c] = yn[c] = T(0);
+    T dt = T(0), t = T(0), h = T(0), wsum = T(0);
+    int att = 0, n_acc = 0, next = 0, flags = 0;
+    int orb = atomicAdd(queue, 1);
+
+    auto load = [&](int o) {
+        const T *base = samples + (int64_t)o * slots;
 #pragma unroll
-            for (int c = 0; c < 6; ++c) yt[c] = y[c] + T(0.5) * dt * k1[c];
-            rhs(P, om, yt, k2);
+        for (int c = 0; c < 6; ++c) {
+            y[c] = w0[c * n_orb + o];
+            k1[c] = base[c * cs];
+        }
+        dt = dt0[o];
+        t = T(0);
+        wsum = T(0);
+        h = sampled ? t_end[o] / T(n_samp) : T(0);
+        att = n_acc = next = flags = 0;
+    };
+    if (orb < n_orb) load(orb);
+
+    while (orb < n_orb) {
+        ++att;
+#pragma unroll 1
+        for (int s = 0; s < 3; ++s) {
+            T yt[6], f[6];
 #pragma unroll
-            for (int c = 0; c < 6; ++c) yt[c] = y[c] + T(0.75) * dt * k2[c];
-            rhs(P, om, yt, k3);
+            for (int c = 0; c < 6; ++c)
+                yt[c] = (s == 0) ? y[c] + T(0.5) * dt * k1[c] : ((s == 1) ? y[c] + T(0.75) * dt * k2[c] : yn[c]);
+            rhs(P, om, yt, f);
+            if (s == 0) {
 #pragma unroll
-            for (int c = 0; c < 6; ++c) yn[c] = y[c] + dt * (b1 * k1[c] + b2 * k2[c] + b3 * k3[c]);
-            T k4[6];
-            rhs(P, om, yn, k4);
-            T s = T(0);
+                for (int c = 0; c < 6; ++c) k2[c] = f[c];
+            } else if (s == 1) {
 #pragma unroll
-            for (int c = 0; c < 6; ++c) {
-                const T err = dt * (e1 * k1[c] + e2 * k2[c] + e3 * k3[c] + e4 * k4[c]);
-                const T ay = M<T>::abs(y[c]), ayn = M<T>::abs(yn[c]);
-                const T sc = I.atol + I.rtol * (ay > ayn ? ay : ayn);
-                const T q = err * M<T>::rcp(sc);
-                s += q * q;
+                for (int c = 0; c < 6; ++c) {
+                    k3[c] = f[c];
+                    yn[c] = y[c] + dt * (b1 * k1[c] + b2 * k2[c] + b3 * f[c]);
+                }
+            } else {
+#pragma unroll
+                for (int c = 0; c < 6; ++c) k4[c] = f[c];
             }
-            const T en = M<T>::sqrt(s / T(6));
-            if (!(en == en)) {   // NaN: the orbit is lost (it fails the E_J test downstream)
-                flags |= 1;
-                break;
-            }
+        }
+        T sq = T(0);
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            const T err = dt * (e1 * k1[c] + e2 * k2[c] + e3 * k3[c] + e4 * k4[c]);
+            const T ay = M<T>::abs(y[c]), ayn = M<T>::abs(yn[c]);
+            const T sc = I.atol + I.rtol * (ay > ayn ? ay : ayn);
+            const T q = err * M<T>::rcp(sc);
+            sq += q * q;
+        }
+        const T en = M<T>::sqrt(sq / T(6));
+        if (!(en == en)) {
+            flags |= 1;   // non-finite: the orbit is lost (it fails the E_J test downstream)
+        } else {
             const bool accept = en <= T(1);
             if (accept) {
                 ++n_acc;
                 const T t1 = t + dt;
                 if (sampled) {
                     const T idt = M<T>::rcp(dt);
-                    // emit all sample times (j + 1/2) h inside (t, t1] by cubic Hermite
-                    while (next < I.n_samples) {
+                    // emit the sample times (j + 1/2) h inside (t, t1] by cubic Hermite
+                    while (next < n_samp) {
                         const T tj = (T(next) + T(0.5)) * h;
                         if (tj > t1) break;
                         const T th = (tj - t) * idt;
@@ -118,12 +168,11 @@ __global__ void __launch_bounds__(128) integrate_kernel(PotT<T> P, IntegT<T> I, 
                         T ys[6];
 #pragma unroll
                         for (int c = 0; c < 6; ++c) ys[c] = h00 * y[c] + h10 * k1[c] + h01 * yn[c] + h11 * k4[c];
-                        if (next < slots) put(samples, n_orb, slots, orb, next, ys, h);
+                        if (next < islots) put(samples, n_orb, slots, orb, next, ys, h);
                         else flags |= 4;
                         wsum += h;
                         ++next;
                     }
-                    stored = next < slots ? next : slots;
                 }
 #pragma unroll
                 for (int c = 0; c < 6; ++c) {
@@ -131,19 +180,19 @@ __global__ void __launch_bounds__(128) integrate_kernel(PotT<T> P, IntegT<T> I, 
                     k1[c] = k4[c];
                 }
                 if (!sampled) {
-                    const int64_t slot = I.store_all ? att - 1 : stored;
-                    if (slot < slots) put(samples, n_orb, slots, orb, slot, y, dt);
+                    const int slot = I.store_all ? att - 1 : next;
+                    if (slot < islots) put(samples, n_orb, slots, orb, slot, y, dt);
                     else flags |= 4;
-                    stored = slot + 1;
+                    next = slot + 1;
                     wsum += dt;
                 }
                 t = t1;
             } else {
                 if (!sampled && I.store_all) {
-                    const int64_t slot = att - 1;
-                    if (slot < slots) put(samples, n_orb, slots, orb, slot, y, T(0));
+                    const int slot = att - 1;
+                    if (slot < islots) put(samples, n_orb, slots, orb, slot, y, T(0));
                     else flags |= 4;
-                    stored = slot + 1;
+                    next = slot + 1;
                 }
                 if (dt <= I.dt_min) {
                     // Rejected at the smallest step: the next attempt repeats this one
@@ -152,29 +201,31 @@ __global__ void __launch_bounds__(128) integrate_kernel(PotT<T> P, IntegT<T> I, 
                     // attempts as the same zero-weight state.
                     flags |= 8;
                     if (!sampled && I.store_all) {
-                        for (int64_t slot = att; slot < att_cap && slot < slots; ++slot)
+                        for (int slot = att; slot < att_cap && slot < islots; ++slot)
                             put(samples, n_orb, slots, orb, slot, y, T(0));
-                        stored = att_cap < slots ? att_cap : slots;
+                        next = att_cap < islots ? att_cap : islots;
                     }
-                    break;
                 }
             }
             T sf = T(0.9) * M<T>::rcbrt(en > T(1e-10) ? en : T(1e-10));
             sf = sf < T(0.2) ? T(0.2) : (sf > T(5) ? T(5) : sf);
-            T dn = dt * sf;
+            const T dn = dt * sf;
             dt = dn < I.dt_min ? I.dt_min : (dn > I.dt_max ? I.dt_max : dn);
         }
-        if (sampled && next < I.n_samples) flags |= 2;
-        if (stored > slots) stored = slots;
-        n_stored[orb] = (int32_t)stored;
-        const T EJ = jacobi(P, om, y);
-        info[SMX_INFO_T * n_orb + orb] = t;
-        info[SMX_INFO_EJ0 * n_orb + orb] = EJ0;
-        info[SMX_INFO_EJ * n_orb + orb] = EJ;
-        info[SMX_INFO_WSUM * n_orb + orb] = wsum;
-        info[SMX_INFO_NACC * n_orb + orb] = T(n_acc);
-        info[SMX_INFO_NATT * n_orb + orb] = T(att);
-        status[orb] = flags;
+        const bool done = (flags & 9) || att >= att_cap || (sampled && next >= n_samp);
+        if (done) {
+            if (sampled && next < n_samp) flags |= 2;
+            n_stored[orb] = next < islots ? next : islots;
+            const T EJ = jacobi(P, om, y);
+            info[SMX_INFO_T * n_orb + orb] = t;
+            info[SMX_INFO_EJ * n_orb + orb] = EJ;
+            info[SMX_INFO_WSUM * n_orb + orb] = wsum;
+            info[SMX_INFO_NACC * n_orb + orb] = T(n_acc);
+            info[SMX_INFO_NATT * n_orb + orb] = T(att);
+            status[orb] = flags;
+            orb = atomicAdd(queue, 1);
+            if (orb < n_orb) load(orb);
+        }
     }
 }
 
@@ -194,6 +245,10 @@ static int launch(const smx_potential *pot, const smx_integrator *cfg, const voi
     I.n_samples = cfg->n_samples;
     I.max_attempts = cfg->max_attempts;
     SMX_TRY_CUDA(cudaMemsetAsync(queue, 0, sizeof(int32_t), s));
+    integrate_init_kernel<T><<<(unsigned)((n_orb + 127) / 128), 128, 0, s>>>(make_pot<T>(*pot), T(cfg->omega),
+                                                                         (const T *)w0, n_orb, slots,
+                                                                         (T *)samples, (T *)info);
+    count_launch();
     int dev = 0, sms = 0;
     SMX_TRY_CUDA(cudaGetDevice(&dev));
     SMX_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
