@@ -149,6 +149,21 @@ int smx_integrate(const smx_potential *pot, const smx_integrator *cfg, int preci
                   int64_t slots, void *samples, int32_t *n_stored, void *info, int32_t *status,
                   int32_t *queue, void *stream);
 
+/* Same as smx_integrate for callers that cannot allocate device memory (a
+ * fixed-pool host runtime, code running where allocation is not allowed, a
+ * binding with no access to the CUDA allocator): the int32 work counter lives
+ * in a 256-byte static device array of the library instead of caller scratch,
+ * so only inputs and outputs are passed.  No counterpart in the reference.
+ * Limits and rules: n_orb <= 2^31 - 2^24 (32-bit counter; larger sizes return
+ * SMX_ERR_UNSUPPORTED); the first call on each device looks up the array's
+ * address (make it before any stream capture); calls share the counter, which
+ * each call zeroes on its stream, so calls that overlap on the GPU race and
+ * must be serialised by the caller.  Allocates nothing. */
+int smx_integrate_noalloc(const smx_potential *pot, const smx_integrator *cfg, int precision,
+                          const void *w0, const void *dt_init, const void *t_total, int64_t n_orb,
+                          int64_t slots, void *samples, int32_t *n_stored, void *info, int32_t *status,
+                          void *stream);
+
 /* ------------------------------------------------------------- projection */
 typedef struct {
     int n_part, n_real;

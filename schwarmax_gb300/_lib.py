@@ -27,7 +27,7 @@ SMX_NNLS_FP64, SMX_NNLS_MIXED = 0, 1
 INFO_T, INFO_EJ0, INFO_EJ, INFO_WSUM, INFO_NACC, INFO_NATT, INFO_FIELDS = range(7)
 
 EXPORTS = ["smx_version", "smx_kernel_launches", "smx_status_string", "smx_last_error", "smx_potential_eval",
-           "smx_initial_conditions", "smx_density_target", "smx_integrate", "smx_project_bin",
+           "smx_initial_conditions", "smx_density_target", "smx_integrate", "smx_integrate_noalloc", "smx_project_bin",
            "smx_sample_cells", "smx_nnls_workspace_size", "smx_nnls_admm", "smx_model_maps", "smx_model_maps_workspace_size"]
 
 
@@ -133,6 +133,8 @@ _SIGS = {
                             ctypes.c_double, ctypes.c_double, _P, ctypes.c_int, _P, _P], ctypes.c_int),
     "smx_integrate": ([ctypes.POINTER(SmxPotential), ctypes.POINTER(SmxIntegrator), ctypes.c_int, _P, _P, _P, _I64,
                        _I64, _P, _P, _P, _P, _P, _P], ctypes.c_int),
+    "smx_integrate_noalloc": ([ctypes.POINTER(SmxPotential), ctypes.POINTER(SmxIntegrator), ctypes.c_int, _P, _P, _P,
+                               _I64, _I64, _P, _P, _P, _P, _P], ctypes.c_int),
     "smx_project_bin": ([ctypes.POINTER(SmxBinning), ctypes.c_int, _P, _P, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _P],
                         ctypes.c_int),
     "smx_sample_cells": ([ctypes.POINTER(SmxBinning), ctypes.c_int, _P, _I64, _P, _P, _P, _P, _P], ctypes.c_int),

@@ -9,6 +9,8 @@
 // Samples are written orbit-major, (7, n_orb, slots), so the projection kernel
 // reads each orbit contiguously; consecutive writes of one thread land in the
 // same sectors and merge in L2.
+#include <mutex>
+
 #include "smx_internal.cuh"
 
 namespace smx {
@@ -291,6 +293,89 @@ extern "C" int smx_integrate(const smx_potential *pot, const smx_integrator *cfg
     if (!(cfg->atol > 0) || !(cfg->rtol >= 0) || !(cfg->dt_min > 0) || !(cfg->dt_max >= cfg->dt_min))
         return set_error(SMX_ERR_ARGUMENT, "bad tolerances or step bounds");
     cudaStream_t s = (cudaStream_t)stream;
+    if (precision == SMX_FP32)
+        return launch<float>(pot, cfg, w0, dt_init, t_total, n_orb, slots, samples, n_stored, info, status, queue, s);
+    if (precision == SMX_FP64)
+        return launch<double>(pot, cfg, w0, dt_init, t_total, n_orb, slots, samples, n_stored, info, status, queue, s);
+    return set_error(SMX_ERR_ARGUMENT, "bad precision %d", precision);
+}
+
+// ---------------------------------------------------------------------------
+// smx_integrate_noalloc: the same integration for callers that cannot allocate
+// device memory themselves (a host runtime with a fixed memory pool, code that
+// runs while allocation is forbidden, a binding without access to the CUDA
+// allocator).  smx_integrate needs one int32 of caller scratch for its work
+// queue; this variant keeps that counter in a static device array of the
+// library instead, so the caller passes only inputs and outputs.
+//
+//   * Scratch: kNoAllocScratchInts int32 (256 bytes) per GPU, held by every
+//     GPU that loads the library until the process exits; one counter is used.
+//   * Limit: the counter is 32-bit, so n_orb is limited to kNoAllocMaxOrbits.
+//   * Set-up: the first call on a device looks up the array's device address
+//     with cudaGetSymbolAddress (the host-side name is only a stand-in); make
+//     that first call before any stream capture.
+//   * Every call zeroes the shared counter on its stream before the kernel;
+//     calls that overlap on the GPU (different streams, or different host
+//     threads on one device) race on it and must be serialised by the caller.
+// ---------------------------------------------------------------------------
+namespace smx {
+
+constexpr int kNoAllocScratchInts = 64;
+constexpr int64_t kNoAllocMaxOrbits = ((int64_t)1 << 31) - ((int64_t)1 << 24);
+constexpr int kNoAllocMaxDevices = 64;
+
+static __device__ __align__(256) int32_t g_noalloc_queue[kNoAllocScratchInts];
+
+static int noalloc_queue_ptr(int32_t **out) {
+    static std::mutex mu;
+    static int32_t *ptrs[kNoAllocMaxDevices] = {nullptr};
+    int dev = 0;
+    SMX_TRY_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices)
+        return set_error(SMX_ERR_UNSUPPORTED, "smx_integrate_noalloc: device %d beyond %d", dev, kNoAllocMaxDevices);
+    std::lock_guard<std::mutex> lock(mu);
+    if (!ptrs[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_queue);
+        if (e != cudaSuccess) return check_cuda(e, "cudaGetSymbolAddress(g_noalloc_queue)");
+        ptrs[dev] = (int32_t *)p;
+    }
+    *out = ptrs[dev];
+    return SMX_OK;
+}
+
+}  // namespace smx
+
+extern "C" int smx_integrate_noalloc(const smx_potential *pot, const smx_integrator *cfg, int precision,
+                                     const void *w0, const void *dt_init, const void *t_total, int64_t n_orb,
+                                     int64_t slots, void *samples, int32_t *n_stored, void *info, int32_t *status,
+                                     void *stream) {
+    int st = validate_potential(pot);
+    if (st) return st;
+    if (!cfg) return set_error(SMX_ERR_ARGUMENT, "smx_integrate_noalloc: cfg is NULL");
+    if (n_orb < 0 || slots < 1) return set_error(SMX_ERR_ARGUMENT, "smx_integrate_noalloc: bad sizes");
+    if (n_orb > kNoAllocMaxOrbits)
+        return set_error(SMX_ERR_UNSUPPORTED,
+                         "smx_integrate_noalloc: n_orb = %lld exceeds the static work counter's limit of %lld orbits",
+                         (long long)n_orb, (long long)kNoAllocMaxOrbits);
+    if (n_orb == 0) return SMX_OK;
+    if (!w0 || !dt_init || !samples || !n_stored || !info || !status)
+        return set_error(SMX_ERR_ARGUMENT, "smx_integrate_noalloc: NULL buffer");
+    if (cfg->mode == SMX_MODE_REFERENCE) {
+        if (cfg->n_attempts < 1) return set_error(SMX_ERR_ARGUMENT, "n_attempts must be >= 1");
+    } else if (cfg->mode == SMX_MODE_SAMPLED) {
+        if (cfg->n_samples < 1 || cfg->max_attempts < 1 || !t_total)
+            return set_error(SMX_ERR_ARGUMENT, "sampled mode needs n_samples, max_attempts and t_total");
+    } else {
+        return set_error(SMX_ERR_ARGUMENT, "unknown integrator mode %d", cfg->mode);
+    }
+    if (!(cfg->atol > 0) || !(cfg->rtol >= 0) || !(cfg->dt_min > 0) || !(cfg->dt_max >= cfg->dt_min))
+        return set_error(SMX_ERR_ARGUMENT, "bad tolerances or step bounds");
+    int32_t *queue = nullptr;
+    st = noalloc_queue_ptr(&queue);
+    if (st) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    // launch<T> zeroes the counter on `s` before the kernel
     if (precision == SMX_FP32)
         return launch<float>(pot, cfg, w0, dt_init, t_total, n_orb, slots, samples, n_stored, info, status, queue, s);
     if (precision == SMX_FP64)
