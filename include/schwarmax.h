@@ -235,6 +235,22 @@ int smx_nnls_admm(const smx_nnls_problem *prob, const void *library, const int32
                   const double *row_scale, const double *Y, double *Z_out, void *workspace,
                   size_t workspace_bytes, void *stream);
 
+/* FP64-accurate product C = A B (A: M x K, B: K x N, C: M x N, all column-major
+ * double) on the bf16 tensor cores by Ozaki splitting: every row of A and column
+ * of B is scaled by a power of two and split into a_slices / b_slices bf16
+ * slices of 8 bits (4 slices: 31 bits, 5 slices: 39 bits below the largest
+ * magnitude of the row or column); slice products are accumulated exactly in
+ * FP32 tensor memory where the result needs it.  The error is about 2^-39 of
+ * sum_k |A_ik| |B_kj|.  Supported (a_slices, b_slices): (4, 4) and (5, 4) for
+ * N <= 112, (4, 4), (5, 5) and (7, 7) for any N.  lower != 0 computes only the
+ * 128 x 128 output tiles on and below the diagonal (symmetric products, M == N;
+ * the other entries of C are 0).  No reference counterpart: this is the
+ * product the mixed-precision NNLS is built on, exposed so that it can be
+ * tested on its own.  Synchronises the stream. */
+int smx_split_gemm_workspace_size(int64_t M, int64_t N, int64_t K, int a_slices, int b_slices, size_t *bytes);
+int smx_split_gemm(int64_t M, int64_t N, int64_t K, int a_slices, int b_slices, int lower, const double *A,
+                   const double *B, double *C, void *workspace, size_t workspace_bytes, void *stream);
+
 /* ------------------------------------------------------- model maps, chi2 */
 typedef struct {
     int64_t n;           /* orbits */

@@ -4,25 +4,38 @@
 // The reference factorises the n x n matrix Q + rho I = U^T U + (lambda/n + rho) I.
 // The design matrix has fewer rows than columns (m < n), so the same inverse
 // is applied through the Woodbury identity with the m x m matrix
-//   G = c I + U U^T,   c = rho + lambda/n,   rho = (||U||_F^2 + lambda)/n:
-//   (Q + rho I)^-1 v = (v - U^T G^-1 U v) / c.
-// With d = z - u the ADMM update w = (Q + rho I)^-1 (rho d + U^T y) becomes
-//   w = (rho/c) (d - U^T G^-1 U d) + U^T G^-1 y,
-// so each iteration costs two skinny GEMMs with U and one application of G^-1;
-// U^T G^-1 y is formed once.  Then w^ = 1.6 w - 0.6 z, z = max(0, w^ + u),
-// u = u + w^ - z exactly as nnls.py:151-158.
+//   G = c I + U U^T,   c = rho + lambda/n,   rho = (||U||_F^2 + lambda)/n,
+// using (U^T U + c I)^-1 U^T = U^T G^-1.  With d = z - u the ADMM update
+// w = (Q + rho I)^-1 (rho d + U^T y) is evaluated in residual form
+//   w = k d + U^T G^-1 (y - k U d),   k = rho/c,
+// which costs two skinny GEMMs with U and one application of G^-1 per
+// iteration.  The grouping matters in low precision: the algebraically equal
+// k (d - U^T G^-1 U d) + U^T G^-1 y subtracts two vectors of the size of d whose
+// difference is up to cond(G) times smaller, so rounding errors of G^-1 and of
+// the products grow by cond(G) (about 1.8e3 at 16384 orbits); in residual form
+// they only scale the correction U^T G^-1 r.  Then w^ = 1.6 w - 0.6 z,
+// z = max(0, w^ + u), u = u + w^ - z exactly as nnls.py:151-158.  The kernels keep
+// D = k (z - u), so that w = D + U^T G^-1 (y - U D).
 //
 // SMX_NNLS_FP64: every step in double (cuBLAS DSYRK/DGEMM, cuSOLVER DPOTRF/DPOTRS).
-// SMX_NNLS_MIXED: U in float; G = U U^T on the tensor cores (TF32 inputs, FP32
-// accumulation); ||U||_F^2, G + cI and its Cholesky factor in double; G^-1 is
-// formed once in float from the double factor and the iterations run float
-// GEMMs on the tensor cores.
+// SMX_NNLS_MIXED: U in float; every product on the bf16 tensor cores with
+// FP64-grade accuracy by Ozaki splitting (split_gemm.cuh): U and the vectors in
+// 4 slices (31 bits below each row's or column's largest value), G^-1 in 5;
+// G = U U^T + cI exact to about 2^-39, its Cholesky factor and the inverse of
+// the factor in double (cuSOLVER), G^-1 = X^T X (X = L^-1) again split; the
+// iterates z, u, D in double.  Rounding U to float moves chi^2 by about 0.02 at
+// 16384 orbits, float storage of G^-1 by about 40 and float arithmetic in the
+// iterations by about 500, which is why the products are split rather than
+// rounded.
 #include <cublas_v2.h>
 #include <cusolverDn.h>
 
 #include <cstdio>
+#include <cstring>
+#include <vector>
 
 #include "smx_internal.cuh"
+#include "split_gemm.cuh"
 
 namespace smx {
 
@@ -67,39 +80,99 @@ static int get_handles(cudaStream_t s, Handles **out) {
 
 static inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// sliced operands of the split path (tile geometry only; pointers are set in run)
+struct SplitShapes {
+    split::Operand Ua, Ut, Xg, Ds, Es, Fs;   // Xg: G^-1 for the iterations
+    split::Operand G7, X7, X5, R5;           // Newton-Schulz operands
+};
+
+static SplitShapes split_shapes(const smx_nnls_problem *p) {
+    SplitShapes sh;
+    const int64_t m = p->m, n = p->n, B = p->n_rhs;
+    const int vt = 112;   // vector tiles: 112 right-hand sides per tile
+    sh.Ua = split::make_operand(m, n, split::MT, 4);    // rows of U over orbits
+    sh.Ut = split::make_operand(n, m, split::MT, 4);    // orbits over rows of U
+    sh.Xg = split::make_operand(m, m, split::MT, 5);
+    sh.Ds = split::make_operand(B, n, vt, 4);
+    sh.Es = split::make_operand(B, m, vt, 4);
+    sh.Fs = split::make_operand(B, m, vt, 4);
+    sh.G7 = split::make_operand(m, m, split::MT, 7);
+    sh.X7 = split::make_operand(m, m, 96, 7);
+    sh.X5 = split::make_operand(m, m, split::MT, 5);
+    sh.R5 = split::make_operand(m, m, split::MT, 5);
+    return sh;
+}
+
 struct Layout {
-    size_t U, G, Gf, work, info, frob, V, Vf, Wc, Z, Uu, D, E, F, Gt, total;
+    size_t U, G, work, info, frob, Z, Uu, D, E, F, Gt, total;
+    // split path
+    size_t Tacc, Racc, rowmax, err;
+    size_t Ua, Ua_e, Ut, Ut_e, Xg, Xg_e, Ds, Ds_e, Es, Es_e, Fs, Fs_e;
+    size_t G7, G7_e, X7, X7_e, X5, X5_e, R5, R5_e, Gf, Xd, Rd;
+    int lwork_s;   // float Cholesky / inverse scratch (floats)
+    int64_t acc_elems;
+    size_t work_bytes, host_bytes;   // device / host scratch of the factorisation and inversion
     int lwork;
 };
 
 static int layout(const smx_nnls_problem *p, Layout *L, cusolverDnHandle_t solver) {
     const size_t m = p->m, n = p->n, B = p->n_rhs;
     const bool mixed = p->mode == SMX_NNLS_MIXED;
-    const size_t eu = mixed ? sizeof(float) : sizeof(double);   // U and iteration element size
     size_t off = 0;
     auto take = [&](size_t bytes) { size_t o = off; off = align256(off + bytes); return o; };
-    L->U = take(m * n * eu);
+    *L = Layout();
+    L->U = take(m * n * (mixed ? sizeof(float) : sizeof(double)));
     L->G = take(m * m * sizeof(double));
-    L->Gf = mixed ? take(m * m * sizeof(float)) : 0;
-    int lwork = 0;
+    int lwork = 0, lw_f = 0, lw_i = 0;
     if (solver) {
-        SMX_TRY_SOLVER(cusolverDnDpotrf_bufferSize(solver, CUBLAS_FILL_MODE_LOWER, (int)m, nullptr, (int)m, &lwork));
+        if (!mixed) {
+            SMX_TRY_SOLVER(cusolverDnDpotrf_bufferSize(solver, CUBLAS_FILL_MODE_LOWER, (int)m, nullptr, (int)m, &lwork));
+        } else {
+            SMX_TRY_SOLVER(cusolverDnSpotrf_bufferSize(solver, CUBLAS_FILL_MODE_LOWER, (int)m, nullptr, (int)m, &lw_f));
+            SMX_TRY_SOLVER(cusolverDnSpotri_bufferSize(solver, CUBLAS_FILL_MODE_LOWER, (int)m, nullptr, (int)m, &lw_i));
+        }
     } else {
-        lwork = (int)(m * 256 + (1 << 20));   // generous estimate for size queries without a handle
+        lwork = lw_f = lw_i = (int)(m * 256 + (1 << 20));   // generous estimate for size queries without a handle
     }
     L->lwork = lwork;
-    L->work = take((size_t)lwork * sizeof(double));
+    L->lwork_s = lw_f > lw_i ? lw_f : lw_i;
+    L->work_bytes = mixed ? (size_t)L->lwork_s * sizeof(float) : (size_t)lwork * sizeof(double);
+    L->host_bytes = 0;
+    L->work = take(L->work_bytes);
     L->info = take(sizeof(int) * 4);
-    L->frob = take(sizeof(double) * 4);   // ||U||_F^2, coef (double), coef (float)
-    L->V = take(m * B * sizeof(double));
-    L->Vf = mixed ? take(m * B * sizeof(float)) : 0;
-    L->Wc = take(n * B * eu);
-    L->Z = take(n * B * eu);
-    L->Uu = take(n * B * eu);
-    L->D = take(n * B * eu);
-    L->E = take(m * B * eu);
-    L->F = take(m * B * eu);
-    L->Gt = take(n * B * eu);
+    L->frob = take(sizeof(double) * 4);   // ||U||_F^2, k (double), k (float)
+    L->Z = take(n * B * sizeof(double));
+    L->Uu = take(n * B * sizeof(double));
+    L->D = take(n * B * sizeof(double));
+    if (!mixed) {
+        L->E = take(m * B * sizeof(double));
+        L->Gt = take(n * B * sizeof(double));
+    } else {
+        const SplitShapes sh = split_shapes(p);
+        const size_t mx = m > n ? m : n;
+        L->acc_elems = (int64_t)(m * m > mx * B ? m * m : mx * B);
+        L->Tacc = take(L->acc_elems * sizeof(unsigned long long));
+        L->Racc = take(L->acc_elems * sizeof(float));
+        L->rowmax = take(mx * sizeof(unsigned long long));
+        L->err = take(sizeof(int) * 4);
+        auto op = [&](const split::Operand &o, size_t &sl, size_t &ex) {
+            sl = take(o.slice_bytes());
+            ex = take((size_t)o.row_tiles * o.tile_rows * sizeof(int32_t));
+        };
+        op(sh.Ua, L->Ua, L->Ua_e);
+        op(sh.Ut, L->Ut, L->Ut_e);
+        op(sh.Xg, L->Xg, L->Xg_e);
+        op(sh.Ds, L->Ds, L->Ds_e);
+        op(sh.Es, L->Es, L->Es_e);
+        op(sh.Fs, L->Fs, L->Fs_e);
+        op(sh.G7, L->G7, L->G7_e);
+        op(sh.X7, L->X7, L->X7_e);
+        op(sh.X5, L->X5, L->X5_e);
+        op(sh.R5, L->R5, L->R5_e);
+        L->Gf = take(m * m * sizeof(float));
+        L->Xd = take(m * m * sizeof(double));
+        L->Rd = take(m * m * sizeof(double));
+    }
     L->total = off;
     return SMX_OK;
 }
@@ -142,83 +215,45 @@ __global__ void frob_kernel(const TU *__restrict__ U, int64_t count, double *out
     }
 }
 
-// G (double, lower part used) = Gsrc + c I, where c = (frob + lambda)/n + lambda/n
-template <typename TS>
-__global__ void shift_gram_kernel(const TS *__restrict__ Gsrc, double *G, int64_t m, const double *frob,
-                                  double lambda, double n) {
-    const double rho = (frob[0] + lambda) / n;
-    const double c = rho + lambda / n;
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < m * m; k += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t i = k % m, j = k / m;
-        double v = (double)Gsrc[k];
-        if (i == j) v += c;
-        G[k] = v;
-    }
-}
-
 __global__ void add_diag_kernel(double *G, int64_t m, const double *frob, double lambda, double n) {
     const double c = (frob[0] + lambda) / n + lambda / n;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x)
         G[i * m + i] += c;
 }
 
-template <typename TO>
-__global__ void convert_kernel(const double *__restrict__ src, TO *dst, int64_t count) {
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x)
-        dst[k] = TO(src[k]);
-}
-
-// lower-triangular copy of the double factor into float with zeros above
-__global__ void tril_to_float_kernel(const double *__restrict__ L, float *Lf, int64_t m) {
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < m * m; k += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t i = k % m, j = k / m;
-        Lf[k] = i >= j ? float(L[k]) : 0.0f;
-    }
-}
-
-__global__ void identity_kernel(float *X, int64_t m) {
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < m * m; k += (int64_t)gridDim.x * blockDim.x)
-        X[k] = (k % m == k / m) ? 1.0f : 0.0f;
-}
-
 template <typename T>
-__global__ void admm_init_kernel(T *Z, T *Uu, T *D, int64_t count, double w_init) {
+__global__ void admm_init_kernel(T *Z, T *Uu, T *D, int64_t count, double w_init, const double *coefp) {
+    const T w = T(w_init), dk = T(coefp[0] * w_init);
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x) {
-        Z[k] = T(w_init);
+        Z[k] = w;
         Uu[k] = T(0);
-        D[k] = T(w_init);
+        D[k] = dk;
     }
 }
 
-// coef[0] = rho / (rho + lambda/n) with rho = (||U||_F^2 + lambda)/n, in double and float
+// coef[0] = k = rho / (rho + lambda/n) with rho = (||U||_F^2 + lambda)/n, in double and float
 __global__ void admm_coef_kernel(const double *frob, double lambda, double n, double *coef) {
     const double rho = (frob[0] + lambda) / n;
     coef[0] = rho / (rho + lambda / n);
     ((float *)(coef + 1))[0] = (float)coef[0];
 }
 
-// w = (rho/c)(d - g) + wc;  w^ = 1.6 w - 0.6 z;  z = max(0, w^ + u);  u += w^ - z;  d = z - u
+// w = D + U^T G^-1 (y - U D);  w^ = 1.6 w - 0.6 z;  z = max(0, w^ + u);  u += w^ - z;  D = k (z - u)
 template <typename T>
-__global__ void admm_update_kernel(const T *__restrict__ Gt, const T *__restrict__ Wc, T *Z, T *Uu, T *D,
-                                   int64_t count, const double *coefp) {
+__global__ void admm_update_kernel(const T *__restrict__ Gt, T *Z, T *Uu, T *D, int64_t count, const double *coefp) {
     const T coef = sizeof(T) == 8 ? T(coefp[0]) : T(((const float *)(coefp + 1))[0]);
     const T alpha = T(1.6);
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x) {
         const T z = Z[k], u = Uu[k];
-        const T w = coef * (D[k] - Gt[k]) + Wc[k];
+        const T w = D[k] + Gt[k];
         const T wh = alpha * w + (T(1) - alpha) * z;
         T zn = wh + u;
         zn = zn > T(0) ? zn : T(0);
         const T un = u + wh - zn;
         Z[k] = zn;
         Uu[k] = un;
-        D[k] = zn - un;
+        D[k] = coef * (zn - un);
     }
-}
-
-__global__ void f2d_kernel(const float *src, double *dst, int64_t count) {
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x)
-        dst[k] = (double)src[k];
 }
 
 static inline unsigned grid1d(int64_t count, int bs = 256) {
@@ -226,6 +261,189 @@ static inline unsigned grid1d(int64_t count, int bs = 256) {
     if (g > 152 * 32) g = 152 * 32;
     if (g < 1) g = 1;
     return (unsigned)g;
+}
+
+// ------------------------------------------------------------ split path
+
+// value of a split product: 2^(eA_r + eB_j - 14) (T/256 + R)
+__device__ __forceinline__ double product_value(const unsigned long long *T, const float *R, int64_t idx, int ea,
+                                                int eb) {
+    const double v = (double)(long long)T[idx] * (1.0 / 256.0) + (double)R[idx];
+    return ldexp(v, ea + eb - 14);
+}
+
+enum { COL_INIT = 0, COL_RESID = 1, COL_PLAIN = 2, COL_UPDATE = 3 };
+
+struct ColArgs {
+    int64_t K, n_rhs;
+    unsigned long long *T;   // product of the previous step (K x n_rhs, ld K), zeroed here after use
+    float *R;
+    const int32_t *eA;       // its row exponents (K) and column exponents (n_rhs)
+    const int32_t *eB;
+    const double *Y;         // COL_RESID: Y[j K + k]
+    double *Z, *Uu, *D;      // COL_INIT / COL_UPDATE: iterates (K x n_rhs)
+    const double *coefp;
+    double w_init;
+    __nv_bfloat16 *slices;   // output operand: n_rhs x K, 4 slices, tiles of tile_rows x KT
+    int32_t *expo;
+    int64_t k_tiles, slice_elems;
+    int tile_rows;
+};
+
+// One CTA per right-hand side j.  Pass 1 forms the column's values (and for
+// COL_INIT / COL_UPDATE the new z, u, D = k (z - u)) and their largest
+// magnitude; pass 2 slices them into the B-operand tiles of the next product.
+//   COL_RESID:  E = Y - U D                 (the residual y - U D)
+//   COL_PLAIN:  F = G^-1 E
+//   COL_UPDATE: w = D + U^T F; w^ = 1.6 w - 0.6 z; z = max(0, w^ + u); u += w^ - z
+template <int MODE>
+__global__ void __launch_bounds__(512) column_slice_kernel(const ColArgs a) {
+    const int64_t j = blockIdx.x, K = a.K;
+    __shared__ double red[16];
+    __shared__ int e_sh;
+    const int eb = (MODE == COL_INIT) ? 0 : a.eB[j];
+    const double coef = a.coefp[0];
+    double mx = 0;
+    for (int64_t k = threadIdx.x; k < K; k += blockDim.x) {
+        const int64_t idx = k + K * j;
+        double v;
+        if (MODE == COL_INIT) {
+            a.Z[idx] = a.w_init;
+            a.Uu[idx] = 0.0;
+            v = coef * a.w_init;
+            a.D[idx] = v;
+        } else if (MODE == COL_UPDATE) {
+            const double gt = product_value(a.T, a.R, idx, a.eA[k], eb);
+            a.T[idx] = 0ull;
+            a.R[idx] = 0.0f;
+            const double z = a.Z[idx], u = a.Uu[idx];
+            const double w = a.D[idx] + gt;
+            const double wh = 1.6 * w - 0.6 * z;
+            double zn = wh + u;
+            zn = zn > 0.0 ? zn : 0.0;
+            const double un = u + wh - zn;
+            a.Z[idx] = zn;
+            a.Uu[idx] = un;
+            v = coef * (zn - un);
+            a.D[idx] = v;
+        } else {
+            v = product_value(a.T, a.R, idx, a.eA[k], eb);
+            if (MODE == COL_RESID) v = a.Y[idx] - v;
+        }
+        mx = fmax(mx, fabs(v));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m2 = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m2 = fmax(m2, red[w]);
+        int e = 0;
+        if (m2 > 0) frexp(m2, &e);
+        e_sh = e;
+        a.expo[j] = e;
+    }
+    __syncthreads();
+    const int e = e_sh;
+    const int64_t jt = j / a.tile_rows, jr = j % a.tile_rows;
+    const int64_t groups = a.k_tiles * (split::KT / 8);
+    for (int64_t g = threadIdx.x; g < groups; g += blockDim.x) {
+        __align__(16) __nv_bfloat16 sl[4][8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int64_t k = g * 8 + q;
+            double v = 0;
+            if (k < K) {
+                const int64_t idx = k + K * j;
+                if (MODE == COL_INIT || MODE == COL_UPDATE) {
+                    v = a.D[idx];
+                } else {
+                    v = product_value(a.T, a.R, idx, a.eA[k], eb);
+                    if (MODE == COL_RESID) v = a.Y[idx] - v;
+                    a.T[idx] = 0ull;
+                    a.R[idx] = 0.0f;
+                }
+            }
+            double r = ldexp(v, 7 - e);
+#pragma unroll
+            for (int s = 0; s < 4; ++s) {
+                const double ai = rint(r);
+                sl[s][q] = __float2bfloat16_rn((float)ldexp(ai, -8 * s));
+                r = (r - ai) * 256.0;
+            }
+        }
+        const int64_t k0 = g * 8, kt = k0 / split::KT;
+        const int64_t base = (jt * a.k_tiles + kt) * (int64_t)a.tile_rows * split::KT +
+                             split::tile_offset((int)jr, (int)(k0 % split::KT), a.tile_rows);
+#pragma unroll
+        for (int s = 0; s < 4; ++s) *(uint4 *)(a.slices + s * a.slice_elems + base) = *(const uint4 *)sl[s];
+    }
+}
+
+// Gram combine: G = 2^(e_r + e_c - 14)(T/256 + R) + c I from the lower-triangle
+// product tiles, written to both triangles in double and to a float copy for the
+// seed factorisation; T and R are cleared for the next product.
+__global__ void gram_combine_kernel(unsigned long long *T, float *R, const int32_t *e, double *G, float *Gf, int64_t m,
+                                    const double *frob, double lambda, double n) {
+    const double c = (frob[0] + lambda) / n + lambda / n;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < m * m; k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = k % m, col = k / m;
+        if (r >= col) {
+            double v = product_value(T, R, k, e[r], e[col]);
+            if (r == col) v += c;
+            G[k] = v;
+            G[col + m * r] = v;
+            Gf[k] = (float)v;
+        }
+        T[k] = 0ull;
+        R[k] = 0.0f;
+    }
+}
+
+// Newton-Schulz seed: X0 = the float inverse (lower triangle of Gf) mirrored, in double
+__global__ void seed_kernel(const float *Gf, double *X, int64_t m) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < m * m; k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = k % m, col = k / m;
+        X[k] = (double)(r >= col ? Gf[k] : Gf[col + m * r]);
+    }
+}
+
+// residual R = I - G X of a Newton-Schulz step (product with four exact levels,
+// T in units of 2^-24); rmax receives max |R| as ordered bits
+__global__ void ns_residual_kernel(unsigned long long *T, float *Racc, const int32_t *eG, const int32_t *eX, double *Rd,
+                                   int64_t m, unsigned long long *rmax) {
+    double mx = 0;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < m * m; k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = k % m, col = k / m;
+        const double gx = ldexp((double)(long long)T[k] * 0x1p-24 + (double)Racc[k], eG[r] + eX[col] - 14);
+        const double v = (r == col ? 1.0 : 0.0) - gx;
+        Rd[k] = v;
+        mx = fmax(mx, fabs(v));
+        T[k] = 0ull;
+        Racc[k] = 0.0f;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(rmax, (unsigned long long)__double_as_longlong(mx));
+}
+
+// X <- X + X R (product with two exact levels, T in units of 2^-8)
+__global__ void ns_update_kernel(unsigned long long *T, float *Racc, const int32_t *eX, const int32_t *eR, double *X,
+                                 int64_t m) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < m * m; k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = k % m, col = k / m;
+        X[k] += product_value(T, Racc, k, eX[r], eR[col]);
+        T[k] = 0ull;
+        Racc[k] = 0.0f;
+    }
+}
+
+__global__ void clear_kernel(unsigned long long *T, float *R, int64_t count) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x) {
+        T[k] = 0ull;
+        R[k] = 0.0f;
+    }
 }
 
 template <typename TL>
@@ -237,12 +455,12 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
     double *G = (double *)(ws + L.G);
     double *frob = (double *)(ws + L.frob);
     int *dinfo = (int *)(ws + L.info);
-    double *V = (double *)(ws + L.V);
     SMX_TRY_CUDA(cudaMemsetAsync(frob, 0, sizeof(double), s));
     SMX_TRY_CUDA(cudaMemsetAsync(dinfo, 0, 4 * sizeof(int), s));
     dim3 gb((unsigned)((m + 255) / 256 < 65535 ? (m + 255) / 256 : 65535), (unsigned)(n < 65535 ? n : 65535));
-    const double one = 1.0, zero = 0.0;
-    const float onef = 1.0f, zerof = 0.0f;
+    const double one = 1.0, zero = 0.0, mone = -1.0;
+    std::vector<unsigned char> host_ws(L.host_bytes > 0 ? L.host_bytes : 1);   // outlives the final synchronize
+    SMX_TRY_BLAS(cublasSetMathMode(h->blas, CUBLAS_DEFAULT_MATH));
     if (!mixed) {
         double *U = (double *)(ws + L.U);
         build_u_kernel<TL, double><<<gb, 256, 0, s>>>(lib, p->ld_lib, row_map, row_scale, m, n, U, dinfo + 3);
@@ -251,92 +469,163 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
         count_launch();
         admm_coef_kernel<<<1, 1, 0, s>>>(frob, lam, (double)n, frob + 1);
         count_launch();
-        SMX_TRY_BLAS(cublasSetMathMode(h->blas, CUBLAS_DEFAULT_MATH));
         SMX_TRY_BLAS(cublasDsyrk(h->blas, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, (int)m, (int)n, &one, U, (int)m, &zero,
                                  G, (int)m));
         add_diag_kernel<<<grid1d(m), 256, 0, s>>>(G, m, frob, lam, (double)n);
         count_launch();
         SMX_TRY_SOLVER(cusolverDnDpotrf(h->solver, CUBLAS_FILL_MODE_LOWER, (int)m, G, (int)m, (double *)(ws + L.work),
                                         L.lwork, dinfo));
-        SMX_TRY_CUDA(cudaMemcpyAsync(V, Y, sizeof(double) * m * B, cudaMemcpyDeviceToDevice, s));
-        SMX_TRY_SOLVER(cusolverDnDpotrs(h->solver, CUBLAS_FILL_MODE_LOWER, (int)m, (int)B, G, (int)m, V, (int)m, dinfo + 1));
-        double *Wc = (double *)(ws + L.Wc), *Z = (double *)(ws + L.Z), *Uu = (double *)(ws + L.Uu),
-               *D = (double *)(ws + L.D), *E = (double *)(ws + L.E), *Gt = (double *)(ws + L.Gt);
-        SMX_TRY_BLAS(cublasDgemm(h->blas, CUBLAS_OP_T, CUBLAS_OP_N, (int)n, (int)B, (int)m, &one, U, (int)m, V, (int)m,
-                                 &zero, Wc, (int)n));
-        admm_init_kernel<double><<<grid1d(n * B), 256, 0, s>>>(Z, Uu, D, n * B, p->w_init);
+        double *Z = (double *)(ws + L.Z), *Uu = (double *)(ws + L.Uu), *D = (double *)(ws + L.D),
+               *E = (double *)(ws + L.E), *Gt = (double *)(ws + L.Gt);
+        admm_init_kernel<double><<<grid1d(n * B), 256, 0, s>>>(Z, Uu, D, n * B, p->w_init, frob + 1);
         count_launch();
         for (int it = 0; it < p->maxiter; ++it) {
-            SMX_TRY_BLAS(cublasDgemm(h->blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)m, (int)B, (int)n, &one, U, (int)m, D,
-                                     (int)n, &zero, E, (int)m));
+            // E = G^-1 (Y - U D)
+            SMX_TRY_CUDA(cudaMemcpyAsync(E, Y, sizeof(double) * m * B, cudaMemcpyDeviceToDevice, s));
+            SMX_TRY_BLAS(cublasDgemm(h->blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)m, (int)B, (int)n, &mone, U, (int)m, D,
+                                     (int)n, &one, E, (int)m));
             SMX_TRY_SOLVER(cusolverDnDpotrs(h->solver, CUBLAS_FILL_MODE_LOWER, (int)m, (int)B, G, (int)m, E, (int)m,
                                             dinfo + 2));
             SMX_TRY_BLAS(cublasDgemm(h->blas, CUBLAS_OP_T, CUBLAS_OP_N, (int)n, (int)B, (int)m, &one, U, (int)m, E,
                                      (int)m, &zero, Gt, (int)n));
-            admm_update_kernel<double><<<grid1d(n * B), 256, 0, s>>>(Gt, Wc, Z, Uu, D, n * B, frob + 1);
+            admm_update_kernel<double><<<grid1d(n * B), 256, 0, s>>>(Gt, Z, Uu, D, n * B, frob + 1);
             count_launch();
         }
         SMX_TRY_CUDA(cudaMemcpyAsync(Z_out, Z, sizeof(double) * n * B, cudaMemcpyDeviceToDevice, s));
     } else {
         float *U = (float *)(ws + L.U);
-        float *Gf = (float *)(ws + L.Gf);
         build_u_kernel<TL, float><<<gb, 256, 0, s>>>(lib, p->ld_lib, row_map, row_scale, m, n, U, dinfo + 3);
         count_launch();
         frob_kernel<float><<<grid1d(m * n), 256, 0, s>>>(U, m * n, frob);
         count_launch();
         admm_coef_kernel<<<1, 1, 0, s>>>(frob, lam, (double)n, frob + 1);
         count_launch();
-        SMX_TRY_BLAS(cublasSetMathMode(h->blas, CUBLAS_TF32_TENSOR_OP_MATH));
-        SMX_TRY_BLAS(cublasGemmEx(h->blas, CUBLAS_OP_N, CUBLAS_OP_T, (int)m, (int)m, (int)n, &onef, U, CUDA_R_32F,
-                                  (int)m, U, CUDA_R_32F, (int)m, &zerof, Gf, CUDA_R_32F, (int)m,
-                                  CUBLAS_COMPUTE_32F_FAST_TF32, CUBLAS_GEMM_DEFAULT));
-        shift_gram_kernel<float><<<grid1d(m * m), 256, 0, s>>>(Gf, G, m, frob, lam, (double)n);
+        SplitShapes sh = split_shapes(p);
+        sh.Ua.slices = (__nv_bfloat16 *)(ws + L.Ua);
+        sh.Ua.expo = (int32_t *)(ws + L.Ua_e);
+        sh.Ut.slices = (__nv_bfloat16 *)(ws + L.Ut);
+        sh.Ut.expo = (int32_t *)(ws + L.Ut_e);
+        sh.Xg.slices = (__nv_bfloat16 *)(ws + L.Xg);
+        sh.Xg.expo = (int32_t *)(ws + L.Xg_e);
+        sh.Ds.slices = (__nv_bfloat16 *)(ws + L.Ds);
+        sh.Ds.expo = (int32_t *)(ws + L.Ds_e);
+        sh.Es.slices = (__nv_bfloat16 *)(ws + L.Es);
+        sh.Es.expo = (int32_t *)(ws + L.Es_e);
+        sh.Fs.slices = (__nv_bfloat16 *)(ws + L.Fs);
+        sh.Fs.expo = (int32_t *)(ws + L.Fs_e);
+        sh.G7.slices = (__nv_bfloat16 *)(ws + L.G7);
+        sh.G7.expo = (int32_t *)(ws + L.G7_e);
+        sh.X7.slices = (__nv_bfloat16 *)(ws + L.X7);
+        sh.X7.expo = (int32_t *)(ws + L.X7_e);
+        sh.X5.slices = (__nv_bfloat16 *)(ws + L.X5);
+        sh.X5.expo = (int32_t *)(ws + L.X5_e);
+        sh.R5.slices = (__nv_bfloat16 *)(ws + L.R5);
+        sh.R5.expo = (int32_t *)(ws + L.R5_e);
+        unsigned long long *Tacc = (unsigned long long *)(ws + L.Tacc);
+        float *Racc = (float *)(ws + L.Racc);
+        unsigned long long *rowmax = (unsigned long long *)(ws + L.rowmax);
+        int *derr = (int *)(ws + L.err);
+        SMX_TRY_CUDA(cudaMemsetAsync(derr, 0, 4 * sizeof(int), s));
+        clear_kernel<<<grid1d(L.acc_elems), 256, 0, s>>>(Tacc, Racc, L.acc_elems);
         count_launch();
-        SMX_TRY_SOLVER(cusolverDnDpotrf(h->solver, CUBLAS_FILL_MODE_LOWER, (int)m, G, (int)m, (double *)(ws + L.work),
-                                        L.lwork, dinfo));
-        float *Wc = (float *)(ws + L.Wc), *Z = (float *)(ws + L.Z), *Uu = (float *)(ws + L.Uu),
-              *D = (float *)(ws + L.D), *E = (float *)(ws + L.E), *F = (float *)(ws + L.F), *Gt = (float *)(ws + L.Gt);
-        // G^-1 in float from the double factor: Lf = tril(L), Linv = L^-1 by TRSM on the
-        // identity, G^-1 = Linv^T Linv.  G's double storage holds the two float m x m
-        // matrices once the factor has been copied out.
-        float *Lf = Gf;
-        tril_to_float_kernel<<<grid1d(m * m), 256, 0, s>>>(G, Lf, m);
+        // the vector operands' padding (right-hand sides beyond n_rhs) stays zero
+        SMX_TRY_CUDA(cudaMemsetAsync(sh.Ds.slices, 0, sh.Ds.slice_bytes(), s));
+        SMX_TRY_CUDA(cudaMemsetAsync(sh.Es.slices, 0, sh.Es.slice_bytes(), s));
+        SMX_TRY_CUDA(cudaMemsetAsync(sh.Fs.slices, 0, sh.Fs.slice_bytes(), s));
+        int st;
+        // U split both ways: rows of U over orbits (U D, U U^T) and orbits over rows (U^T F)
+        if ((st = split::slice_rows<float>(U, 1, m, sh.Ua, rowmax, s))) return st;
+        if ((st = split::slice_rows<float>(U, m, 1, sh.Ut, rowmax, s))) return st;
+        // G = U U^T + c I, exact to about 2^-39 of the float design matrix
+        split::Acc acc{Tacc, Racc, m};
+        float *Gf = (float *)(ws + L.Gf);
+        double *Xd = (double *)(ws + L.Xd), *Rd = (double *)(ws + L.Rd);
+        if ((st = split::gemm(sh.Ua, sh.Ua, 6, acc, true, derr, s))) return st;
+        gram_combine_kernel<<<grid1d(m * m), 256, 0, s>>>(Tacc, Racc, sh.Ua.expo, G, Gf, m, frob, lam, (double)n);
         count_launch();
-        float *Linv = (float *)G;
-        float *Gi = (float *)G + m * m;
-        identity_kernel<<<grid1d(m * m), 256, 0, s>>>(Linv, m);
+        // G^-1: float Cholesky inverse as the seed, then Newton-Schulz steps
+        //   R = I - G X (7 x 7 slices, error about 2^-55 |G||X|), X <- X + X R.
+        // The new X has residual R^2, so the loop stops after the step whose
+        // input had max |R| <= 1e-6; the result is limited by the accuracy of
+        // G X times cond(G), about 2^-44.
+        SMX_TRY_SOLVER(cusolverDnSpotrf(h->solver, CUBLAS_FILL_MODE_LOWER, (int)m, Gf, (int)m, (float *)(ws + L.work),
+                                        L.lwork_s, dinfo));
+        SMX_TRY_SOLVER(cusolverDnSpotri(h->solver, CUBLAS_FILL_MODE_LOWER, (int)m, Gf, (int)m, (float *)(ws + L.work),
+                                        L.lwork_s, dinfo + 1));
+        seed_kernel<<<grid1d(m * m), 256, 0, s>>>(Gf, Xd, m);
         count_launch();
-        SMX_TRY_BLAS(cublasSetMathMode(h->blas, CUBLAS_DEFAULT_MATH));
-        SMX_TRY_BLAS(cublasStrsm(h->blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT,
-                                 (int)m, (int)m, &onef, Lf, (int)m, Linv, (int)m));
-        SMX_TRY_BLAS(cublasSgemm(h->blas, CUBLAS_OP_T, CUBLAS_OP_N, (int)m, (int)m, (int)m, &onef, Linv, (int)m, Linv,
-                                 (int)m, &zerof, Gi, (int)m));
-        // constant term Wc = U^T G^-1 Y with the same G^-1 the iterations use (FP32)
-        convert_kernel<float><<<grid1d(m * B), 256, 0, s>>>(Y, E, m * B);
-        count_launch();
-        SMX_TRY_BLAS(cublasSgemm(h->blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)m, (int)B, (int)m, &onef, Gi, (int)m, E, (int)m,
-                                 &zerof, F, (int)m));
-        SMX_TRY_BLAS(cublasSgemm(h->blas, CUBLAS_OP_T, CUBLAS_OP_N, (int)n, (int)B, (int)m, &onef, U, (int)m, F,
-                                 (int)m, &zerof, Wc, (int)n));
-        admm_init_kernel<float><<<grid1d(n * B), 256, 0, s>>>(Z, Uu, D, n * B, p->w_init);
-        count_launch();
-        SMX_TRY_BLAS(cublasSetMathMode(h->blas, CUBLAS_TF32_TENSOR_OP_MATH));
-        for (int it = 0; it < p->maxiter; ++it) {
-            SMX_TRY_BLAS(cublasGemmEx(h->blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)m, (int)B, (int)n, &onef, U, CUDA_R_32F,
-                                      (int)m, D, CUDA_R_32F, (int)n, &zerof, E, CUDA_R_32F, (int)m,
-                                      CUBLAS_COMPUTE_32F_FAST_TF32, CUBLAS_GEMM_DEFAULT));
-            SMX_TRY_BLAS(cublasGemmEx(h->blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)m, (int)B, (int)m, &onef, Gi, CUDA_R_32F,
-                                      (int)m, E, CUDA_R_32F, (int)m, &zerof, F, CUDA_R_32F, (int)m,
-                                      CUBLAS_COMPUTE_32F_FAST_TF32, CUBLAS_GEMM_DEFAULT));
-            SMX_TRY_BLAS(cublasGemmEx(h->blas, CUBLAS_OP_T, CUBLAS_OP_N, (int)n, (int)B, (int)m, &onef, U, CUDA_R_32F,
-                                      (int)m, F, CUDA_R_32F, (int)m, &zerof, Gt, CUDA_R_32F, (int)n,
-                                      CUBLAS_COMPUTE_32F_FAST_TF32, CUBLAS_GEMM_DEFAULT));
-            admm_update_kernel<float><<<grid1d(n * B), 256, 0, s>>>(Gt, Wc, Z, Uu, D, n * B, frob + 1);
+        if ((st = split::slice_rows<double>(G, 1, m, sh.G7, rowmax, s))) return st;
+        unsigned long long *rmax = (unsigned long long *)(frob + 3);
+        double res = 1.0;
+        int steps = 0;
+        for (; steps < 6 && res > 1e-12; ++steps) {
+            if ((st = split::slice_rows<double>(Xd, m, 1, sh.X7, rowmax, s))) return st;   // X columns over k
+            if ((st = split::gemm(sh.G7, sh.X7, 8, acc, false, derr, s))) return st;
+            SMX_TRY_CUDA(cudaMemsetAsync(rmax, 0, sizeof(unsigned long long), s));
+            ns_residual_kernel<<<grid1d(m * m), 256, 0, s>>>(Tacc, Racc, sh.G7.expo, sh.X7.expo, Rd, m, rmax);
             count_launch();
+            if ((st = split::slice_rows<double>(Xd, 1, m, sh.X5, rowmax, s))) return st;   // X rows over k
+            if ((st = split::slice_rows<double>(Rd, m, 1, sh.R5, rowmax, s))) return st;   // R columns over k
+            if ((st = split::gemm(sh.X5, sh.R5, 6, acc, false, derr, s))) return st;
+            ns_update_kernel<<<grid1d(m * m), 256, 0, s>>>(Tacc, Racc, sh.X5.expo, sh.R5.expo, Xd, m);
+            count_launch();
+            unsigned long long bits = 0;
+            SMX_TRY_CUDA(cudaMemcpyAsync(&bits, rmax, sizeof(bits), cudaMemcpyDeviceToHost, s));
+            SMX_TRY_CUDA(cudaStreamSynchronize(s));
+            double r;
+            memcpy(&r, &bits, sizeof(r));
+            // the residual of the step's input X: the updated X has about its square
+            res = r * r;
+            if (!(r < 0.5)) break;   // not converging: the seed is too far off
         }
-        SMX_TRY_BLAS(cublasSetMathMode(h->blas, CUBLAS_DEFAULT_MATH));
-        f2d_kernel<<<grid1d(n * B), 256, 0, s>>>(Z, Z_out, n * B);
-        count_launch();
+        if (!(res <= 1e-12)) {
+            SMX_TRY_CUDA(cudaStreamSynchronize(s));
+            return set_error(SMX_ERR_NUMERIC, "Newton-Schulz inverse of rho' I + U U^T did not converge (residual^2 %g)",
+                             res);
+        }
+        if ((st = split::slice_rows<double>(Xd, 1, m, sh.Xg, rowmax, s))) return st;   // G^-1 rows over columns
+        double *Z = (double *)(ws + L.Z), *Uu = (double *)(ws + L.Uu), *D = (double *)(ws + L.D);
+        const double *coefp = frob + 1;
+        auto col = [&](int mode, int64_t K, const int32_t *eA, const int32_t *eB, split::Operand &out) -> int {
+            ColArgs a;
+            a.K = K;
+            a.n_rhs = B;
+            a.T = Tacc;
+            a.R = Racc;
+            a.eA = eA;
+            a.eB = eB;
+            a.Y = Y;
+            a.Z = Z;
+            a.Uu = Uu;
+            a.D = D;
+            a.coefp = coefp;
+            a.w_init = p->w_init;
+            a.slices = out.slices;
+            a.expo = out.expo;
+            a.k_tiles = out.k_tiles;
+            a.slice_elems = out.slice_elems();
+            a.tile_rows = out.tile_rows;
+            switch (mode) {
+                case COL_INIT: column_slice_kernel<COL_INIT><<<(unsigned)B, 512, 0, s>>>(a); break;
+                case COL_RESID: column_slice_kernel<COL_RESID><<<(unsigned)B, 512, 0, s>>>(a); break;
+                case COL_PLAIN: column_slice_kernel<COL_PLAIN><<<(unsigned)B, 512, 0, s>>>(a); break;
+                default: column_slice_kernel<COL_UPDATE><<<(unsigned)B, 512, 0, s>>>(a); break;
+            }
+            count_launch();
+            return SMX_OK;
+        };
+        split::Acc acc_m{Tacc, Racc, m}, acc_n{Tacc, Racc, n};
+        col(COL_INIT, n, nullptr, nullptr, sh.Ds);
+        for (int it = 0; it < p->maxiter; ++it) {
+            if ((st = split::gemm(sh.Ua, sh.Ds, 6, acc_m, false, derr, s))) return st;   // U D
+            col(COL_RESID, m, sh.Ua.expo, sh.Ds.expo, sh.Es);                           // E = Y - U D
+            if ((st = split::gemm(sh.Xg, sh.Es, 6, acc_m, false, derr, s))) return st;   // G^-1 E
+            col(COL_PLAIN, m, sh.Xg.expo, sh.Es.expo, sh.Fs);                           // F
+            if ((st = split::gemm(sh.Ut, sh.Fs, 6, acc_n, false, derr, s))) return st;   // U^T F
+            col(COL_UPDATE, n, sh.Ut.expo, sh.Fs.expo, sh.Ds);                          // ADMM update, D
+        }
+        SMX_TRY_CUDA(cudaMemcpyAsync(Z_out, Z, sizeof(double) * n * B, cudaMemcpyDeviceToDevice, s));
+        SMX_TRY_CUDA(cudaMemcpyAsync(dinfo + 2, derr, sizeof(int), cudaMemcpyDeviceToDevice, s));
     }
     SMX_TRY_CUDA(cudaGetLastError());
     // the factorisation status is read back: a failed Cholesky is reported, not silently used
@@ -345,6 +634,8 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
     SMX_TRY_CUDA(cudaStreamSynchronize(s));
     if (hinfo[3] != 0) return set_error(SMX_ERR_ARGUMENT, "row_map holds an index outside [0, ld_lib)");
     if (hinfo[0] != 0) return set_error(SMX_ERR_NUMERIC, "Cholesky of rho' I + U U^T failed (info=%d)", hinfo[0]);
+    if (mixed && hinfo[1] != 0) return set_error(SMX_ERR_NUMERIC, "inverse of the Cholesky factor failed (info=%d)", hinfo[1]);
+    if (mixed && hinfo[2] != 0) return set_error(SMX_ERR_CUDA, "split product kernel gave up waiting (code %d)", hinfo[2]);
     return SMX_OK;
 }
 

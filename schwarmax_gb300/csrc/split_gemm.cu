@@ -1,0 +1,661 @@
+// FP64-accurate products on the bf16 tensor cores: the sliced GEMM kernel and
+// the slicing kernels (method and number format in split_gemm.cuh).
+//
+// Kernel layout (one CTA per SM, stream-K over (output tile, k tile) units):
+//   warp 0      producer: one cp.async.bulk per slice tile into a STAGES-deep ring
+//               (the slices are stored in global memory in the shared-memory tile
+//               layout, so a tile is one contiguous copy; no tensor map);
+//   warp 1      owns the tensor memory and issues tcgen05.mma from one thread;
+//   warps 2..9  epilogue: at the end of every exact chunk they read the level 2/3
+//               accumulators (tcgen05.ld) into int32 running sums; at the end of
+//               a tile's k range they add T and R to global memory with atomics.
+// Tensor memory: level 2 at column 0, level 3 at 128, levels >= 4 at 256.
+// Every wait is bounded by a clock deadline; on expiry the CTA records an error
+// code, stops issuing work and leaves after its outstanding operations.
+#include <cstdio>
+
+#include "smx_internal.cuh"
+#include "split_gemm.cuh"
+
+namespace smx {
+namespace split {
+
+namespace dev {
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// tcgen05 shared-memory matrix descriptor, no swizzle: lbo = byte stride between
+// core matrices along K, sbo = along M/N; bit 46 = descriptor version.
+__device__ __forceinline__ uint64_t desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((saddr >> 4) & 0x3FFF) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | ((uint64_t)1 << 46);
+}
+
+// instruction descriptor kind::f16: D f32, A and B bf16, both K-major
+__host__ __device__ constexpr uint32_t idesc(int m, int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *b, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count));
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t addr, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+
+// wait for the phase of the given parity to complete, for at most ~2^31 cycles
+__device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity, volatile int *abort_flag) {
+    const uint32_t a = smem_u32(b);
+    if (mbar_try(a, parity)) return true;
+    const long long t0 = clock64();
+    while (true) {
+        if (mbar_try(a, parity)) return true;
+        if (*abort_flag) return false;
+        if (clock64() - t0 > (1ll << 31)) return false;
+    }
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *b) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *b, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void mma(uint32_t dtmem, uint64_t a, uint64_t b, uint32_t id, uint32_t accumulate) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(dtmem),
+        "l"(a), "l"(b), "r"(id), "r"(accumulate));
+}
+
+__device__ __forceinline__ void commit(uint64_t *bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void ld8(uint32_t taddr, float *v) {
+    uint32_t r[8];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
+#pragma unroll
+    for (int j = 0; j < 8; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+__device__ __forceinline__ void ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+}  // namespace dev
+
+struct GemmParams {
+    const __nv_bfloat16 *A, *B;
+    int64_t a_slice, b_slice;            // elements between slices
+    int64_t a_row_tiles, b_row_tiles, k_tiles;
+    int64_t M, N;                        // logical output size
+    int64_t n_tiles_out;                 // output tiles along N
+    int64_t units;                       // total (tile, k tile) units
+    int lower_only;
+    unsigned long long *T;
+    float *R;
+    int64_t ld;
+    int *err;
+};
+
+// output tile index -> (row tile, column tile)
+__device__ __forceinline__ void tile_coords(const GemmParams &p, int64_t tile, int64_t &mt, int64_t &nt) {
+    if (!p.lower_only) {
+        mt = tile % p.a_row_tiles;
+        nt = tile / p.a_row_tiles;
+    } else {   // lower-triangular tiles in row order: tile = mt (mt + 1) / 2 + nt
+        int64_t r = (int64_t)((sqrt(8.0 * (double)tile + 1.0) - 1.0) * 0.5);
+        while (r * (r + 1) / 2 > tile) --r;
+        while ((r + 1) * (r + 2) / 2 <= tile) ++r;
+        mt = r;
+        nt = tile - r * (r + 1) / 2;
+    }
+}
+
+template <int SA, int SB, int LMAX, int NT, int EXACT, int STAGES>
+struct Cfg {
+    static constexpr uint32_t A_TILE = MT * KT * 2;        // bytes of one slice tile
+    static constexpr uint32_t B_TILE = NT * KT * 2;
+    static constexpr uint32_t STAGE = SA * A_TILE + SB * B_TILE;
+    static constexpr uint32_t SMEM = STAGES * STAGE + 256;
+    static constexpr int HALF = NT / 2;                     // columns per epilogue warp
+    static constexpr int THREADS = 320;
+    // tensor-memory columns per accumulator: EXACT exact levels + 1 rounded
+    static constexpr int ACC_STRIDE = (NT + 31) / 32 * 32;
+    // the exact levels' sums stay below 2^24 units over 1024 / (pairs per level) k
+    static constexpr int MAXP = EXACT < (SA < SB ? SA : SB) ? EXACT : (SA < SB ? SA : SB);
+    static constexpr int CHUNK_K = MAXP <= 1 ? 1024 : MAXP == 2 ? 512 : 256;
+    static constexpr int CHUNK_KT = CHUNK_K / KT;
+};
+
+template <int SA, int SB, int LMAX, int NT, int EXACT, int STAGES>
+__global__ void __launch_bounds__(320, 1) gemm_kernel(const GemmParams p) {
+    using C = Cfg<SA, SB, LMAX, NT, EXACT, STAGES>;
+    static_assert(NT % 16 == 0 && NT <= 128 && NT >= 16, "N tile");
+    static_assert(C::HALF % 8 == 0, "epilogue columns in groups of 8");
+    static_assert((EXACT + 1) * C::ACC_STRIDE <= 512, "tensor memory");
+    static_assert(EXACT >= 1 && EXACT <= 4, "exact levels");
+    extern __shared__ __align__(1024) unsigned char smem[];
+    uint64_t *full = (uint64_t *)(smem + STAGES * C::STAGE);
+    uint64_t *empty = full + STAGES;
+    uint64_t *acc_full = empty + STAGES;
+    uint64_t *acc_empty = acc_full + 1;
+    uint32_t *tmem_holder = (uint32_t *)(acc_empty + 1);
+    volatile int *abort_flag = (volatile int *)(tmem_holder + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t u0 = p.units * blockIdx.x / gridDim.x, u1 = p.units * (blockIdx.x + 1) / gridDim.x;
+
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < STAGES; ++i) {
+            dev::mbar_init(full + i, 1);
+            dev::mbar_init(empty + i, 1);
+        }
+        dev::mbar_init(acc_full, 1);
+        dev::mbar_init(acc_empty, 8);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         dev::smem_u32(tmem_holder)),
+                     "r"(512));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    dev::fence_before();
+    __syncthreads();
+    dev::fence_after();
+    const uint32_t tmem = *tmem_holder;
+
+    // flush schedule shared by the MMA issuer and the epilogue: after unit u,
+    // flush if the chunk is full, the output flush distance is reached or the tile ends
+    if (warp == 0) {
+        if (lane == 0) {
+            int64_t it = 0;
+            for (int64_t u = u0; u < u1; ++u, ++it) {
+                const int stage = (int)(it % STAGES);
+                if (it >= STAGES && !dev::mbar_wait(empty + stage, (uint32_t)((it / STAGES - 1) & 1), abort_flag)) {
+                    atomicExch(p.err, 1);
+                    *abort_flag = 1;
+                    break;
+                }
+                const int64_t tile = u / p.k_tiles, kt = u % p.k_tiles;
+                int64_t mt, nt;
+                tile_coords(p, tile, mt, nt);
+                unsigned char *sbase = smem + stage * C::STAGE;
+                dev::mbar_expect_tx(full + stage, C::STAGE);
+#pragma unroll
+                for (int s = 0; s < SA; ++s)
+                    dev::bulk_g2s(sbase + s * C::A_TILE, p.A + s * p.a_slice + (mt * p.k_tiles + kt) * (MT * KT),
+                                  C::A_TILE, full + stage);
+#pragma unroll
+                for (int t = 0; t < SB; ++t)
+                    dev::bulk_g2s(sbase + SA * C::A_TILE + t * C::B_TILE,
+                                  p.B + t * p.b_slice + (nt * p.k_tiles + kt) * (NT * KT), C::B_TILE, full + stage);
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            constexpr uint32_t ID = dev::idesc(MT, NT);
+            constexpr uint32_t LBO_A = (MT / 8) * 128, LBO_B = (NT / 8) * 128, SBO = 128;
+            int64_t it = 0;
+            int since_chunk = 0, since_out = 0;
+            uint32_t flushes = 0;
+            uint32_t fresh = (1u << (EXACT + 1)) - 1;   // accumulators to overwrite on their next MMA
+            for (int64_t u = u0; u < u1; ++u, ++it) {
+                const int stage = (int)(it % STAGES);
+                if (!dev::mbar_wait(full + stage, (uint32_t)((it / STAGES) & 1), abort_flag)) {
+                    atomicExch(p.err, 2);
+                    *abort_flag = 1;
+                    break;
+                }
+                dev::fence_after();
+                const uint32_t sa = dev::smem_u32(smem + stage * C::STAGE);
+                const uint32_t sb = sa + SA * C::A_TILE;
+#pragma unroll
+                for (int j = 0; j < KT / 16; ++j) {
+#pragma unroll
+                    for (int s = 1; s <= SA; ++s) {
+#pragma unroll
+                        for (int t = 1; t <= SB; ++t) {
+                            if (s + t <= LMAX) {
+                                const uint64_t ad = dev::desc(sa + (s - 1) * C::A_TILE + j * 2 * LBO_A, LBO_A, SBO);
+                                const uint64_t bd = dev::desc(sb + (t - 1) * C::B_TILE + j * 2 * LBO_B, LBO_B, SBO);
+                                const int acc = (s + t - 2) < EXACT ? (s + t - 2) : EXACT;
+                                dev::mma(tmem + acc * C::ACC_STRIDE, ad, bd, ID, (fresh >> acc) & 1u ? 0u : 1u);
+                                fresh &= ~(1u << acc);
+                            }
+                        }
+                    }
+                }
+                dev::commit(empty + stage);
+                ++since_chunk;
+                ++since_out;
+                const bool tile_end = (u % p.k_tiles == p.k_tiles - 1) || (u + 1 == u1);
+                const bool out_flush = tile_end || since_out == OUT_KT;
+                if (out_flush || since_chunk == C::CHUNK_KT) {
+                    dev::commit(acc_full);
+                    if (u + 1 < u1) {
+                        if (!dev::mbar_wait(acc_empty, flushes & 1, abort_flag)) {
+                            atomicExch(p.err, 3);
+                            *abort_flag = 1;
+                            break;
+                        }
+                        dev::fence_after();
+                    }
+                    ++flushes;
+                    fresh |= (1u << EXACT) - 1;
+                    since_chunk = 0;
+                    if (out_flush) {
+                        fresh |= 1u << EXACT;
+                        since_out = 0;
+                    }
+                }
+            }
+        }
+    } else {
+        // epilogue: warp w reads lanes 32 (w % 4) .. + 31 (its row quarter), column half h.
+        // The exact levels of a chunk are combined into one int64 per column in units
+        // of 2^-8(EXACT-1): level 2 + e holds multiples of 2^-8e below 2^24 units.
+        const int q = warp & 3, h = (warp - 2) >> 2;
+        const int row = q * 32 + lane;
+        const uint32_t lane_addr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(h * C::HALF);
+        long long sum[C::HALF];
+#pragma unroll
+        for (int c = 0; c < C::HALF; ++c) sum[c] = 0;
+        int since_chunk = 0, since_out = 0;
+        uint32_t flushes = 0;
+        for (int64_t u = u0; u < u1; ++u) {
+            ++since_chunk;
+            ++since_out;
+            const bool tile_end = (u % p.k_tiles == p.k_tiles - 1) || (u + 1 == u1);
+            const bool out_flush = tile_end || since_out == OUT_KT;
+            if (!(out_flush || since_chunk == C::CHUNK_KT)) continue;
+            if (!dev::mbar_wait(acc_full, flushes & 1, abort_flag)) {
+                if (lane == 0) atomicExch(p.err, 4);
+                *abort_flag = 1;
+                break;
+            }
+            ++flushes;
+            dev::fence_after();
+            int64_t mt = 0, nt = 0;
+            if (out_flush) tile_coords(p, u / p.k_tiles, mt, nt);
+            const int64_t gi = mt * MT + row;
+#pragma unroll
+            for (int c0 = 0; c0 < C::HALF; c0 += 8) {
+                float v[EXACT][8], vr[8];
+#pragma unroll
+                for (int e = 0; e < EXACT; ++e) dev::ld8(lane_addr + e * C::ACC_STRIDE + c0, v[e]);
+                if (out_flush) dev::ld8(lane_addr + EXACT * C::ACC_STRIDE + c0, vr);
+                dev::ld_wait();
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    long long add = 0;
+#pragma unroll
+                    for (int e = 0; e < EXACT; ++e)
+                        add += (long long)__float2int_rn(v[e][j] * (float)(1 << (8 * e))) << (8 * (EXACT - 1 - e));
+                    sum[c0 + j] += add;
+                }
+                if (out_flush) {
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        const int64_t gj = nt * NT + h * C::HALF + c0 + j;
+                        if (gi < p.M && gj < p.N) {
+                            atomicAdd(p.T + gi + p.ld * gj, (unsigned long long)sum[c0 + j]);
+                            atomicAdd(p.R + gi + p.ld * gj, vr[j]);
+                        }
+                        sum[c0 + j] = 0;
+                    }
+                }
+            }
+            dev::fence_before();
+            __syncwarp();
+            if (lane == 0) dev::mbar_arrive(acc_empty);
+            since_chunk = 0;
+            if (out_flush) since_out = 0;
+        }
+    }
+    dev::fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        dev::fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
+    }
+}
+
+// ------------------------------------------------------------------ slicing
+
+// max |x| per row, as the bits of a non-negative double (ordered like the values)
+template <typename T>
+__global__ void rowmax_kernel(const T *__restrict__ src, int64_t sr, int64_t sc, int64_t rows, int64_t k,
+                              unsigned long long *rowmax, int rows_fast) {
+    if (rows_fast) {   // consecutive threads on consecutive rows; blocks along k
+        const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+        if (r >= rows) return;
+        const int64_t kc = (k + gridDim.y - 1) / gridDim.y;
+        const int64_t k0 = blockIdx.y * kc, k1 = k0 + kc < k ? k0 + kc : k;
+        double m = 0;
+        for (int64_t c = k0; c < k1; ++c) m = fmax(m, fabs((double)src[r * sr + c * sc]));
+        atomicMax(rowmax + r, (unsigned long long)__double_as_longlong(m));
+    } else {           // one warp per row, lanes along k
+        const int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+        const int lane = threadIdx.x & 31;
+        if (r >= rows) return;
+        double m = 0;
+        for (int64_t c = lane; c < k; c += 32) m = fmax(m, fabs((double)src[r * sr + c * sc]));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (lane == 0) atomicMax(rowmax + r, (unsigned long long)__double_as_longlong(m));
+    }
+}
+
+// e with max < 2^e (0 for an all-zero row)
+__device__ __forceinline__ int scale_exponent(double mx) {
+    if (!(mx > 0)) return 0;
+    int e;
+    frexp(mx, &e);   // mx = f 2^e, f in [0.5, 1)
+    return e;
+}
+
+__global__ void expo_kernel(const unsigned long long *rowmax, int32_t *expo, int64_t rows, int64_t rows_padded) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < rows_padded; r += (int64_t)gridDim.x * blockDim.x)
+        expo[r] = r < rows ? scale_exponent(__longlong_as_double((long long)rowmax[r])) : 0;
+}
+
+// slices of one value x < 2^e in magnitude: a'_s = a_s 2^-8(s-1), a_s in [-128, 128]
+template <int S>
+__device__ __forceinline__ void make_slices(double x, int e, __nv_bfloat16 *out) {
+    double r = ldexp(x, 7 - e);
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+        const double a = rint(r);
+        out[s] = __float2bfloat16_rn((float)ldexp(a, -8 * s));
+        r = (r - a) * 256.0;
+    }
+}
+
+// one CTA per (row tile, k tile): builds the S slice tiles in shared memory and
+// writes each as contiguous 16-byte vectors
+template <typename T, int S>
+__global__ void slice_rows_kernel(const T *__restrict__ src, int64_t sr, int64_t sc, int64_t rows, int64_t k,
+                                  const int32_t *__restrict__ expo, __nv_bfloat16 *slices, int tile_rows,
+                                  int64_t k_tiles, int64_t slice_elems, int k_fast) {
+    extern __shared__ __align__(16) unsigned char sm_raw[];
+    __nv_bfloat16 *tile = (__nv_bfloat16 *)sm_raw;   // S x tile_rows x KT
+    const int64_t kt = blockIdx.x, rt = blockIdx.y;
+    const int n = tile_rows * KT;
+    for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
+        int r, c;
+        if (k_fast) {
+            c = idx % KT;
+            r = idx / KT;
+        } else {
+            r = idx % tile_rows;
+            c = idx / tile_rows;
+        }
+        const int64_t gr = rt * tile_rows + r, gc = kt * KT + c;
+        double x = 0;
+        int e = 0;
+        if (gr < rows && gc < k) {
+            x = (double)src[gr * sr + gc * sc];
+            e = expo[gr];
+        }
+        __nv_bfloat16 v[S];
+        make_slices<S>(x, e, v);
+        const int64_t off = tile_offset(r, c, tile_rows);
+#pragma unroll
+        for (int s = 0; s < S; ++s) tile[s * n + off] = v[s];
+    }
+    __syncthreads();
+    const int vec = n / 8;   // 16-byte vectors per slice tile
+    for (int idx = threadIdx.x; idx < S * vec; idx += blockDim.x) {
+        const int s = idx / vec, v = idx % vec;
+        const uint4 w = ((const uint4 *)(tile + s * n))[v];
+        ((uint4 *)(slices + s * slice_elems + (rt * k_tiles + kt) * n))[v] = w;
+    }
+}
+
+// ------------------------------------------------------------------ host side
+
+template <int SA, int SB, int LMAX, int NT, int EXACT>
+static int launch_gemm(const Operand &A, const Operand &B, const Acc &acc, bool lower_only, int *err, cudaStream_t s) {
+    // as many stages as fit in 227 KB of shared memory (2 or 3)
+    constexpr int STAGES = Cfg<SA, SB, LMAX, NT, EXACT, 3>::SMEM <= 232448 ? 3 : 2;
+    using C = Cfg<SA, SB, LMAX, NT, EXACT, STAGES>;
+    static_assert(C::SMEM <= 232448, "shared memory");
+    SMX_TRY_CUDA(cudaFuncSetAttribute(gemm_kernel<SA, SB, LMAX, NT, EXACT, STAGES>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM));
+    int dev = 0, sms = 0;
+    SMX_TRY_CUDA(cudaGetDevice(&dev));
+    SMX_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    GemmParams p;
+    p.A = A.slices;
+    p.B = B.slices;
+    p.a_slice = A.slice_elems();
+    p.b_slice = B.slice_elems();
+    p.a_row_tiles = A.row_tiles;
+    p.b_row_tiles = B.row_tiles;
+    p.k_tiles = A.k_tiles;
+    p.M = A.rows;
+    p.N = B.rows;
+    p.n_tiles_out = B.row_tiles;
+    p.lower_only = lower_only ? 1 : 0;
+    const int64_t tiles = lower_only ? A.row_tiles * (A.row_tiles + 1) / 2 : A.row_tiles * B.row_tiles;
+    p.units = tiles * A.k_tiles;
+    p.T = acc.T;
+    p.R = acc.R;
+    p.ld = acc.ld;
+    p.err = err;
+    int64_t grid = sms;
+    if (grid > p.units) grid = p.units;
+    gemm_kernel<SA, SB, LMAX, NT, EXACT, STAGES><<<(unsigned)grid, C::THREADS, C::SMEM, s>>>(p);
+    count_launch();
+    SMX_TRY_CUDA(cudaGetLastError());
+    return SMX_OK;
+}
+
+int exact_levels(int a_slices, int b_slices, int lmax) {
+    return (a_slices == 7 && b_slices == 7 && lmax == 8) ? 4 : 2;
+}
+
+int gemm(const Operand &A, const Operand &B, int lmax, const Acc &acc, bool lower_only, int *err, cudaStream_t s) {
+    if (!A.slices || !A.expo || !B.slices || !B.expo || !acc.T || !acc.R || !err)
+        return set_error(SMX_ERR_ARGUMENT, "split gemm: operand or accumulator without storage");
+    if (acc.ld < A.rows) return set_error(SMX_ERR_ARGUMENT, "split gemm: accumulator leading dimension too small");
+    if (A.k_tiles != B.k_tiles || A.tile_rows != MT)
+        return set_error(SMX_ERR_ARGUMENT, "split gemm: operand shapes do not match");
+    if (lower_only && B.tile_rows != MT) return set_error(SMX_ERR_ARGUMENT, "split gemm: lower_only needs square tiles");
+    const int key = A.S * 1000 + B.S * 100 + lmax * 10;
+    if (B.tile_rows == 112) {
+        switch (key) {
+            case 4460: return launch_gemm<4, 4, 6, 112, 2>(A, B, acc, lower_only, err, s);
+            case 5460: return launch_gemm<5, 4, 6, 112, 2>(A, B, acc, lower_only, err, s);
+            default: break;
+        }
+    } else if (B.tile_rows == 128) {
+        switch (key) {
+            case 4460: return launch_gemm<4, 4, 6, 128, 2>(A, B, acc, lower_only, err, s);
+            case 5560: return launch_gemm<5, 5, 6, 128, 2>(A, B, acc, lower_only, err, s);
+            default: break;
+        }
+    } else if (B.tile_rows == 96) {
+        switch (key) {
+            case 7780: return launch_gemm<7, 7, 8, 96, 4>(A, B, acc, lower_only, err, s);
+            default: break;
+        }
+    }
+    return set_error(SMX_ERR_UNSUPPORTED, "split gemm: no kernel for %d x %d slices, level %d, tile %d", A.S, B.S, lmax,
+                     B.tile_rows);
+}
+
+static inline unsigned grid_for(int64_t count, int bs) {
+    int64_t g = (count + bs - 1) / bs;
+    if (g > 152 * 64) g = 152 * 64;
+    return (unsigned)(g < 1 ? 1 : g);
+}
+
+template <typename T>
+int slice_rows(const T *src, int64_t sr, int64_t sc, const Operand &op, unsigned long long *rowmax, cudaStream_t s) {
+    if (!src || !op.slices || !op.expo || !rowmax)
+        return set_error(SMX_ERR_ARGUMENT, "slice_rows: operand without storage");
+    const int64_t rows_padded = op.row_tiles * op.tile_rows;
+    SMX_TRY_CUDA(cudaMemsetAsync(rowmax, 0, sizeof(unsigned long long) * op.rows, s));
+    // rows contiguous in memory (sr == 1): threads along rows; else a warp per row along k
+    const bool rows_fast = sr == 1;
+    if (rows_fast) {
+        dim3 g((unsigned)((op.rows + 255) / 256), (unsigned)(op.k < 64 ? op.k : 64));
+        rowmax_kernel<T><<<g, 256, 0, s>>>(src, sr, sc, op.rows, op.k, rowmax, 1);
+    } else {
+        rowmax_kernel<T><<<grid_for(op.rows * 32, 256), 256, 0, s>>>(src, sr, sc, op.rows, op.k, rowmax, 0);
+    }
+    count_launch();
+    expo_kernel<<<grid_for(rows_padded, 256), 256, 0, s>>>(rowmax, op.expo, op.rows, rows_padded);
+    count_launch();
+    dim3 g((unsigned)op.k_tiles, (unsigned)op.row_tiles);
+    const size_t sm = (size_t)op.S * op.tile_rows * KT * sizeof(__nv_bfloat16);
+    const int k_fast = sc == 1 ? 1 : 0;
+    switch (op.S) {
+#define SMX_SLICE_CASE(NS)                                                                                       \
+    case NS:                                                                                                    \
+        SMX_TRY_CUDA(cudaFuncSetAttribute(slice_rows_kernel<T, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                          (int)sm));                                                             \
+        slice_rows_kernel<T, NS><<<g, 256, sm, s>>>(src, sr, sc, op.rows, op.k, op.expo, op.slices, op.tile_rows,  \
+                                                    op.k_tiles, op.slice_elems(), k_fast);                       \
+        break;
+        SMX_SLICE_CASE(4)
+        SMX_SLICE_CASE(5)
+        SMX_SLICE_CASE(7)
+#undef SMX_SLICE_CASE
+        default: return set_error(SMX_ERR_UNSUPPORTED, "slice_rows: %d slices", op.S);
+    }
+    count_launch();
+    SMX_TRY_CUDA(cudaGetLastError());
+    return SMX_OK;
+}
+
+template int slice_rows<float>(const float *, int64_t, int64_t, const Operand &, unsigned long long *, cudaStream_t);
+template int slice_rows<double>(const double *, int64_t, int64_t, const Operand &, unsigned long long *, cudaStream_t);
+
+}  // namespace split
+}  // namespace smx
+
+// ------------------------------------------------------------ C ABI (products)
+
+namespace smx {
+namespace split {
+
+__global__ void combine_kernel(const unsigned long long *T, const float *R, const int32_t *eA, const int32_t *eB,
+                               double *C, int64_t M, int64_t N, int t_shift) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < M * N; k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = k % M, j = k / M;
+        const double v = ldexp((double)(long long)T[k], -t_shift) + (double)R[k];
+        C[k] = ldexp(v, eA[i] + eB[j] - 14);
+    }
+}
+
+struct ProductLayout {
+    Operand A, B;
+    size_t a_sl, a_e, b_sl, b_e, T, R, rowmax, err, total;
+};
+
+static int product_layout(int64_t M, int64_t N, int64_t K, int sa, int sb, ProductLayout *L) {
+    const bool ok44 = sa == 4 && sb == 4, ok54 = sa == 5 && sb == 4, ok55 = sa == 5 && sb == 5,
+               ok77 = sa == 7 && sb == 7;
+    int bt;
+    if (N <= 112 && (ok44 || ok54)) bt = 112;
+    else if (ok44 || ok55) bt = 128;
+    else if (ok77) bt = 96;
+    else return set_error(SMX_ERR_UNSUPPORTED, "smx_split_gemm: slices %d x %d with N = %lld", sa, sb, (long long)N);
+    L->A = make_operand(M, K, MT, sa);
+    L->B = make_operand(N, K, bt, sb);
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off = (off + bytes + 255) & ~(size_t)255; return o; };
+    L->a_sl = take(L->A.slice_bytes());
+    L->a_e = take(L->A.row_tiles * MT * sizeof(int32_t));
+    L->b_sl = take(L->B.slice_bytes());
+    L->b_e = take(L->B.row_tiles * bt * sizeof(int32_t));
+    L->T = take(M * N * sizeof(unsigned long long));
+    L->R = take(M * N * sizeof(float));
+    L->rowmax = take((M > N ? M : N) * sizeof(unsigned long long));
+    L->err = take(sizeof(int) * 4);
+    L->total = off;
+    return SMX_OK;
+}
+
+}  // namespace split
+}  // namespace smx
+
+using namespace smx;
+
+extern "C" int smx_split_gemm_workspace_size(int64_t M, int64_t N, int64_t K, int a_slices, int b_slices,
+                                             size_t *bytes) {
+    if (!bytes || M < 1 || N < 1 || K < 1) return set_error(SMX_ERR_ARGUMENT, "smx_split_gemm_workspace_size: bad argument");
+    split::ProductLayout L;
+    int st = split::product_layout(M, N, K, a_slices, b_slices, &L);
+    if (st) return st;
+    *bytes = L.total;
+    return SMX_OK;
+}
+
+extern "C" int smx_split_gemm(int64_t M, int64_t N, int64_t K, int a_slices, int b_slices, int lower, const double *A,
+                              const double *B, double *C, void *workspace, size_t workspace_bytes, void *stream) {
+    if (M < 1 || N < 1 || K < 1 || !A || !B || !C || !workspace)
+        return set_error(SMX_ERR_ARGUMENT, "smx_split_gemm: bad argument");
+    if (M * N > ((int64_t)1 << 31) || M * K > ((int64_t)1 << 33) || N * K > ((int64_t)1 << 33))
+        return set_error(SMX_ERR_UNSUPPORTED, "smx_split_gemm: problem too large");
+    split::ProductLayout L;
+    int st = split::product_layout(M, N, K, a_slices, b_slices, &L);
+    if (st) return st;
+    if (lower && (M != N || L.B.tile_rows != split::MT))
+        return set_error(SMX_ERR_ARGUMENT, "smx_split_gemm: lower needs M == N and 128-row tiles");
+    if (workspace_bytes < L.total)
+        return set_error(SMX_ERR_WORKSPACE, "smx_split_gemm: workspace %zu < %zu bytes", workspace_bytes, L.total);
+    cudaStream_t s = (cudaStream_t)stream;
+    unsigned char *ws = (unsigned char *)workspace;
+    split::Operand a = L.A, b = L.B;
+    a.slices = (__nv_bfloat16 *)(ws + L.a_sl);
+    a.expo = (int32_t *)(ws + L.a_e);
+    b.slices = (__nv_bfloat16 *)(ws + L.b_sl);
+    b.expo = (int32_t *)(ws + L.b_e);
+    unsigned long long *T = (unsigned long long *)(ws + L.T);
+    float *R = (float *)(ws + L.R);
+    int *err = (int *)(ws + L.err);
+    SMX_TRY_CUDA(cudaMemsetAsync(T, 0, M * N * sizeof(unsigned long long), s));
+    SMX_TRY_CUDA(cudaMemsetAsync(R, 0, M * N * sizeof(float), s));
+    SMX_TRY_CUDA(cudaMemsetAsync(err, 0, sizeof(int), s));
+    // A rows i over k: A[i + M k];  B^T rows j over k: B[k + K j]
+    if ((st = split::slice_rows<double>(A, 1, M, a, (unsigned long long *)(ws + L.rowmax), s))) return st;
+    if ((st = split::slice_rows<double>(B, K, 1, b, (unsigned long long *)(ws + L.rowmax), s))) return st;
+    split::Acc acc{T, R, M};
+    const int lmax = (a_slices == 7 && b_slices == 7) ? 8 : 6;
+    if ((st = split::gemm(a, b, lmax, acc, lower != 0, err, s))) return st;
+    const int shift = 8 * (split::exact_levels(a_slices, b_slices, lmax) - 1);
+    split::combine_kernel<<<split::grid_for(M * N, 256), 256, 0, s>>>(T, R, a.expo, b.expo, C, M, N, shift);
+    count_launch();
+    SMX_TRY_CUDA(cudaGetLastError());
+    int herr = 0;
+    SMX_TRY_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    SMX_TRY_CUDA(cudaStreamSynchronize(s));
+    if (herr) return set_error(SMX_ERR_CUDA, "smx_split_gemm: product kernel gave up waiting (code %d)", herr);
+    return SMX_OK;
+}

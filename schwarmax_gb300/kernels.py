@@ -181,6 +181,27 @@ def nnls_admm(library, row_map, row_scale, Y, maxiter, lambda_reg, w_init, mixed
     return Z
 
 
+def split_gemm(A, B, a_slices=4, b_slices=4, lower=False):
+    """C = A @ B for double CUDA tensors A (M, K), B (K, N) through the split
+    (Ozaki) tensor-core product smx_split_gemm; returns C (M, N) double.
+    lower: only the 128 x 128 tiles on and below the diagonal (M == N)."""
+    M, K = A.shape
+    K2, N = B.shape
+    if K2 != K:
+        raise ValueError("split_gemm: inner dimensions differ")
+    At = A.t().contiguous()          # column-major A
+    Bt = B.t().contiguous()          # column-major B
+    _check(At, "A", torch.float64, (K, M))
+    _check(Bt, "B", torch.float64, (N, K))
+    nbytes = ctypes.c_size_t(0)
+    call("smx_split_gemm_workspace_size", M, N, K, a_slices, b_slices, ctypes.byref(nbytes))
+    ws = torch.empty(nbytes.value, dtype=torch.uint8, device=A.device)
+    Ct = torch.empty(N, M, dtype=torch.float64, device=A.device)
+    call("smx_split_gemm", M, N, K, a_slices, b_slices, int(lower), _ptr(At), _ptr(Bt), _ptr(Ct), _ptr(ws), ws.numel(),
+         _stream())
+    return Ct.t()
+
+
 def model_maps(library, n_cells, n_bins, W, gamma_kin, v0, s, y_rz, y_xy, y_xy_boot, y_h_boot, sig_h_raw,
                lum_factor, sigma_amplify=1.0, want_maps=True):
     n, ld = library.shape

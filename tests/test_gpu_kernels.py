@@ -402,10 +402,17 @@ def _nnls_inputs(c, w=(math.sqrt(5.0), math.sqrt(5.0), 1.0)):
     return row_map, rs, Y
 
 
-@pytest.mark.parametrize("mixed,tol", [(False, 1e-9), (True, 2e-3)])
+@pytest.mark.parametrize("mixed,tol", [(False, 1e-9), (True, 2e-7)])
 def test_nnls_admm_matches_oracle(K, mixed, tol):
+    """FP64 and mixed (split tensor-core products) ADMM against the oracle.  The
+    mixed path takes a float library, so the oracle gets the same float-rounded
+    design matrices; what remains is the solver's own error."""
     rng = np.random.default_rng(18)
     c = _nnls_case(rng)
+    if mixed:
+        c = dict(c, A_rz=c["A_rz"].astype(np.float32).astype(np.float64),
+                 A_xy=c["A_xy"].astype(np.float32).astype(np.float64),
+                 A_h=c["A_h"].astype(np.float32).astype(np.float64))
     w = (math.sqrt(5.0), math.sqrt(5.0), 1.0)
     ref = onnls.solve_nnls_admm_bootstrap(c["A_rz"], c["A_xy"], *c["A_h"][1:], c["y_rz"], c["y_xy"], c["gamma"],
                                           c["y_xy_b"], *c["y_h_b"], c["sig_rz"], c["sig_xy"], *c["sig_h"],
