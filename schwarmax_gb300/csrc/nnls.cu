@@ -19,14 +19,15 @@
 //
 // SMX_NNLS_FP64: every step in double (cuBLAS DSYRK/DGEMM, cuSOLVER DPOTRF/DPOTRS).
 // SMX_NNLS_MIXED: U in float; every product on the bf16 tensor cores with
-// FP64-grade accuracy by Ozaki splitting (split_gemm.cuh): U and the vectors in
-// 4 slices (31 bits below each row's or column's largest value), G^-1 in 5;
-// G = U U^T + cI exact to about 2^-39, its Cholesky factor and the inverse of
-// the factor in double (cuSOLVER), G^-1 = X^T X (X = L^-1) again split; the
-// iterates z, u, D in double.  Rounding U to float moves chi^2 by about 0.02 at
-// 16384 orbits, float storage of G^-1 by about 40 and float arithmetic in the
-// iterations by about 500, which is why the products are split rather than
-// rounded.
+// FP64-grade accuracy by Ozaki splitting (split_gemm.cuh): U in 4 slices (31 bits
+// below each row's or column's largest magnitude), the iterates' vectors in 5
+// (39 bits), G^-1 in 5.  G = U U^T + cI is formed from the slices of U; G^-1
+// starts from a float Cholesky inverse and is refined by Newton-Schulz steps
+// whose residual products use 7 slices; the iterates z, u, D stay in double.
+// At 16384 orbits (cond(G) = 1.8e3) the weights move the chi^2 by about 0.02
+// when U is rounded to float, by about 40 when G^-1 is stored in float and by
+// about 500 when the iterations run in float arithmetic, which is why the
+// products are split rather than rounded.
 #include <cublas_v2.h>
 #include <cusolverDn.h>
 
@@ -93,9 +94,9 @@ static SplitShapes split_shapes(const smx_nnls_problem *p) {
     sh.Ua = split::make_operand(m, n, split::MT, 4);    // rows of U over orbits
     sh.Ut = split::make_operand(n, m, split::MT, 4);    // orbits over rows of U
     sh.Xg = split::make_operand(m, m, split::MT, 5);
-    sh.Ds = split::make_operand(B, n, vt, 4);
-    sh.Es = split::make_operand(B, m, vt, 4);
-    sh.Fs = split::make_operand(B, m, vt, 4);
+    sh.Ds = split::make_operand(B, n, vt, 5);
+    sh.Es = split::make_operand(B, m, 64, 5);   // G^-1 E: 64-wide tiles, five exact levels
+    sh.Fs = split::make_operand(B, m, vt, 5);
     sh.G7 = split::make_operand(m, m, split::MT, 7);
     sh.X7 = split::make_operand(m, m, 96, 7);
     sh.X5 = split::make_operand(m, m, split::MT, 5);
@@ -108,7 +109,7 @@ struct Layout {
     // split path
     size_t Tacc, Racc, rowmax, err;
     size_t Ua, Ua_e, Ut, Ut_e, Xg, Xg_e, Ds, Ds_e, Es, Es_e, Fs, Fs_e;
-    size_t G7, G7_e, X7, X7_e, X5, X5_e, R5, R5_e, Gf, Xd, Rd;
+    size_t G7, G7_e, X7, X7_e, X5, X5_e, R5, R5_e, Gf, Xd, Rd, Ebuf, gdiag;
     int lwork_s;   // float Cholesky / inverse scratch (floats)
     int64_t acc_elems;
     size_t work_bytes, host_bytes;   // device / host scratch of the factorisation and inversion
@@ -172,6 +173,8 @@ static int layout(const smx_nnls_problem *p, Layout *L, cusolverDnHandle_t solve
         L->Gf = take(m * m * sizeof(float));
         L->Xd = take(m * m * sizeof(double));
         L->Rd = take(m * m * sizeof(double));
+        L->Ebuf = take(m * B * sizeof(double));
+        L->gdiag = take(m * sizeof(double));
     }
     L->total = off;
     return SMX_OK;
@@ -265,10 +268,10 @@ static inline unsigned grid1d(int64_t count, int bs = 256) {
 
 // ------------------------------------------------------------ split path
 
-// value of a split product: 2^(eA_r + eB_j - 14) (T/256 + R)
+// value of a split product: 2^(eA_r + eB_j - 14) (T 2^-t_shift + R), t_shift = 8 (exact levels - 1)
 __device__ __forceinline__ double product_value(const unsigned long long *T, const float *R, int64_t idx, int ea,
-                                                int eb) {
-    const double v = (double)(long long)T[idx] * (1.0 / 256.0) + (double)R[idx];
+                                                int eb, int t_shift = 16) {
+    const double v = ldexp((double)(long long)T[idx], -t_shift) + (double)R[idx];
     return ldexp(v, ea + eb - 14);
 }
 
@@ -281,21 +284,26 @@ struct ColArgs {
     const int32_t *eA;       // its row exponents (K) and column exponents (n_rhs)
     const int32_t *eB;
     const double *Y;         // COL_RESID: Y[j K + k]
+    double *E;               // COL_RESID writes E, COL_PLAIN reads it (K x n_rhs)
+    const double *g;         // COL_PLAIN: diagonal of G^-1, applied exactly
     double *Z, *Uu, *D;      // COL_INIT / COL_UPDATE: iterates (K x n_rhs)
     const double *coefp;
     double w_init;
-    __nv_bfloat16 *slices;   // output operand: n_rhs x K, 4 slices, tiles of tile_rows x KT
+    __nv_bfloat16 *slices;   // output operand: n_rhs x K, VS slices, tiles of tile_rows x KT
     int32_t *expo;
     int64_t k_tiles, slice_elems;
     int tile_rows;
+    int t_shift;             // units of the product's T: 2^-t_shift
 };
 
 // One CTA per right-hand side j.  Pass 1 forms the column's values (and for
 // COL_INIT / COL_UPDATE the new z, u, D = k (z - u)) and their largest
 // magnitude; pass 2 slices them into the B-operand tiles of the next product.
 //   COL_RESID:  E = Y - U D                 (the residual y - U D)
-//   COL_PLAIN:  F = G^-1 E
+//   COL_PLAIN:  F = g E + O E               (G^-1 = diag(g) + O; O E is the product)
 //   COL_UPDATE: w = D + U^T F; w^ = 1.6 w - 0.6 z; z = max(0, w^ + u); u += w^ - z
+constexpr int VS = 5;   // slices of the vector operands: 39 bits below each column's largest magnitude
+
 template <int MODE>
 __global__ void __launch_bounds__(512) column_slice_kernel(const ColArgs a) {
     const int64_t j = blockIdx.x, K = a.K;
@@ -313,7 +321,7 @@ __global__ void __launch_bounds__(512) column_slice_kernel(const ColArgs a) {
             v = coef * a.w_init;
             a.D[idx] = v;
         } else if (MODE == COL_UPDATE) {
-            const double gt = product_value(a.T, a.R, idx, a.eA[k], eb);
+            const double gt = product_value(a.T, a.R, idx, a.eA[k], eb, a.t_shift);
             a.T[idx] = 0ull;
             a.R[idx] = 0.0f;
             const double z = a.Z[idx], u = a.Uu[idx];
@@ -327,8 +335,13 @@ __global__ void __launch_bounds__(512) column_slice_kernel(const ColArgs a) {
             v = coef * (zn - un);
             a.D[idx] = v;
         } else {
-            v = product_value(a.T, a.R, idx, a.eA[k], eb);
-            if (MODE == COL_RESID) v = a.Y[idx] - v;
+            v = product_value(a.T, a.R, idx, a.eA[k], eb, a.t_shift);
+            if (MODE == COL_RESID) {
+                v = a.Y[idx] - v;
+                a.E[idx] = v;
+            } else {
+                v += a.g[k] * a.E[idx];
+            }
         }
         mx = fmax(mx, fabs(v));
     }
@@ -349,7 +362,7 @@ __global__ void __launch_bounds__(512) column_slice_kernel(const ColArgs a) {
     const int64_t jt = j / a.tile_rows, jr = j % a.tile_rows;
     const int64_t groups = a.k_tiles * (split::KT / 8);
     for (int64_t g = threadIdx.x; g < groups; g += blockDim.x) {
-        __align__(16) __nv_bfloat16 sl[4][8];
+        __align__(16) __nv_bfloat16 sl[VS][8];
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
             const int64_t k = g * 8 + q;
@@ -359,15 +372,15 @@ __global__ void __launch_bounds__(512) column_slice_kernel(const ColArgs a) {
                 if (MODE == COL_INIT || MODE == COL_UPDATE) {
                     v = a.D[idx];
                 } else {
-                    v = product_value(a.T, a.R, idx, a.eA[k], eb);
-                    if (MODE == COL_RESID) v = a.Y[idx] - v;
+                    v = product_value(a.T, a.R, idx, a.eA[k], eb, a.t_shift);
+                    v = (MODE == COL_RESID) ? a.Y[idx] - v : v + a.g[k] * a.E[idx];
                     a.T[idx] = 0ull;
                     a.R[idx] = 0.0f;
                 }
             }
             double r = ldexp(v, 7 - e);
 #pragma unroll
-            for (int s = 0; s < 4; ++s) {
+            for (int s = 0; s < VS; ++s) {
                 const double ai = rint(r);
                 sl[s][q] = __float2bfloat16_rn((float)ldexp(ai, -8 * s));
                 r = (r - ai) * 256.0;
@@ -377,7 +390,7 @@ __global__ void __launch_bounds__(512) column_slice_kernel(const ColArgs a) {
         const int64_t base = (jt * a.k_tiles + kt) * (int64_t)a.tile_rows * split::KT +
                              split::tile_offset((int)jr, (int)(k0 % split::KT), a.tile_rows);
 #pragma unroll
-        for (int s = 0; s < 4; ++s) *(uint4 *)(a.slices + s * a.slice_elems + base) = *(const uint4 *)sl[s];
+        for (int s = 0; s < VS; ++s) *(uint4 *)(a.slices + s * a.slice_elems + base) = *(const uint4 *)sl[s];
     }
 }
 
@@ -428,7 +441,7 @@ __global__ void ns_residual_kernel(unsigned long long *T, float *Racc, const int
     if ((threadIdx.x & 31) == 0) atomicMax(rmax, (unsigned long long)__double_as_longlong(mx));
 }
 
-// X <- X + X R (product with two exact levels, T in units of 2^-8)
+// X <- X + X R
 __global__ void ns_update_kernel(unsigned long long *T, float *Racc, const int32_t *eX, const int32_t *eR, double *X,
                                  int64_t m) {
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < m * m; k += (int64_t)gridDim.x * blockDim.x) {
@@ -436,6 +449,16 @@ __global__ void ns_update_kernel(unsigned long long *T, float *Racc, const int32
         X[k] += product_value(T, Racc, k, eX[r], eR[col]);
         T[k] = 0ull;
         Racc[k] = 0.0f;
+    }
+}
+
+// G^-1 = diag(g) + O: the diagonal dominates its rows (about 14x the largest
+// off-diagonal entry at 16384 orbits), so it is applied exactly in double and
+// only O goes through the split product, whose row scales then follow O.
+__global__ void split_diag_kernel(double *X, double *g, int64_t m) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < m; r += (int64_t)gridDim.x * blockDim.x) {
+        g[r] = X[r + m * r];
+        X[r + m * r] = 0.0;
     }
 }
 
@@ -540,7 +563,7 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
         split::Acc acc{Tacc, Racc, m};
         float *Gf = (float *)(ws + L.Gf);
         double *Xd = (double *)(ws + L.Xd), *Rd = (double *)(ws + L.Rd);
-        if ((st = split::gemm(sh.Ua, sh.Ua, 6, acc, true, derr, s))) return st;
+        if ((st = split::gemm(sh.Ua, sh.Ua, acc, true, derr, s))) return st;
         gram_combine_kernel<<<grid1d(m * m), 256, 0, s>>>(Tacc, Racc, sh.Ua.expo, G, Gf, m, frob, lam, (double)n);
         count_launch();
         // G^-1: float Cholesky inverse as the seed, then Newton-Schulz steps
@@ -560,13 +583,13 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
         int steps = 0;
         for (; steps < 6 && res > 1e-12; ++steps) {
             if ((st = split::slice_rows<double>(Xd, m, 1, sh.X7, rowmax, s))) return st;   // X columns over k
-            if ((st = split::gemm(sh.G7, sh.X7, 8, acc, false, derr, s))) return st;
+            if ((st = split::gemm(sh.G7, sh.X7, acc, false, derr, s))) return st;
             SMX_TRY_CUDA(cudaMemsetAsync(rmax, 0, sizeof(unsigned long long), s));
             ns_residual_kernel<<<grid1d(m * m), 256, 0, s>>>(Tacc, Racc, sh.G7.expo, sh.X7.expo, Rd, m, rmax);
             count_launch();
             if ((st = split::slice_rows<double>(Xd, 1, m, sh.X5, rowmax, s))) return st;   // X rows over k
             if ((st = split::slice_rows<double>(Rd, m, 1, sh.R5, rowmax, s))) return st;   // R columns over k
-            if ((st = split::gemm(sh.X5, sh.R5, 6, acc, false, derr, s))) return st;
+            if ((st = split::gemm(sh.X5, sh.R5, acc, false, derr, s))) return st;
             ns_update_kernel<<<grid1d(m * m), 256, 0, s>>>(Tacc, Racc, sh.X5.expo, sh.R5.expo, Xd, m);
             count_launch();
             unsigned long long bits = 0;
@@ -583,10 +606,14 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
             return set_error(SMX_ERR_NUMERIC, "Newton-Schulz inverse of rho' I + U U^T did not converge (residual^2 %g)",
                              res);
         }
-        if ((st = split::slice_rows<double>(Xd, 1, m, sh.Xg, rowmax, s))) return st;   // G^-1 rows over columns
+        double *gdiag = (double *)(ws + L.gdiag), *Ebuf = (double *)(ws + L.Ebuf);
+        split_diag_kernel<<<grid1d(m), 256, 0, s>>>(Xd, gdiag, m);
+        count_launch();
+        if ((st = split::slice_rows<double>(Xd, 1, m, sh.Xg, rowmax, s))) return st;   // O rows over columns
         double *Z = (double *)(ws + L.Z), *Uu = (double *)(ws + L.Uu), *D = (double *)(ws + L.D);
         const double *coefp = frob + 1;
-        auto col = [&](int mode, int64_t K, const int32_t *eA, const int32_t *eB, split::Operand &out) -> int {
+        auto col = [&](int mode, int64_t K, const int32_t *eA, const int32_t *eB, split::Operand &out,
+                       int t_shift) -> int {
             ColArgs a;
             a.K = K;
             a.n_rhs = B;
@@ -595,6 +622,8 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
             a.eA = eA;
             a.eB = eB;
             a.Y = Y;
+            a.E = Ebuf;
+            a.g = gdiag;
             a.Z = Z;
             a.Uu = Uu;
             a.D = D;
@@ -605,6 +634,7 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
             a.k_tiles = out.k_tiles;
             a.slice_elems = out.slice_elems();
             a.tile_rows = out.tile_rows;
+            a.t_shift = t_shift;
             switch (mode) {
                 case COL_INIT: column_slice_kernel<COL_INIT><<<(unsigned)B, 512, 0, s>>>(a); break;
                 case COL_RESID: column_slice_kernel<COL_RESID><<<(unsigned)B, 512, 0, s>>>(a); break;
@@ -615,14 +645,17 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
             return SMX_OK;
         };
         split::Acc acc_m{Tacc, Racc, m}, acc_n{Tacc, Racc, n};
-        col(COL_INIT, n, nullptr, nullptr, sh.Ds);
+        const int sh_ud = 8 * (split::exact_levels(sh.Ua, sh.Ds) - 1);
+        const int sh_ge = 8 * (split::exact_levels(sh.Xg, sh.Es) - 1);
+        const int sh_uf = 8 * (split::exact_levels(sh.Ut, sh.Fs) - 1);
+        col(COL_INIT, n, nullptr, nullptr, sh.Ds, 0);
         for (int it = 0; it < p->maxiter; ++it) {
-            if ((st = split::gemm(sh.Ua, sh.Ds, 6, acc_m, false, derr, s))) return st;   // U D
-            col(COL_RESID, m, sh.Ua.expo, sh.Ds.expo, sh.Es);                           // E = Y - U D
-            if ((st = split::gemm(sh.Xg, sh.Es, 6, acc_m, false, derr, s))) return st;   // G^-1 E
-            col(COL_PLAIN, m, sh.Xg.expo, sh.Es.expo, sh.Fs);                           // F
-            if ((st = split::gemm(sh.Ut, sh.Fs, 6, acc_n, false, derr, s))) return st;   // U^T F
-            col(COL_UPDATE, n, sh.Ut.expo, sh.Fs.expo, sh.Ds);                          // ADMM update, D
+            if ((st = split::gemm(sh.Ua, sh.Ds, acc_m, false, derr, s))) return st;   // U D
+            col(COL_RESID, m, sh.Ua.expo, sh.Ds.expo, sh.Es, sh_ud);                    // E = Y - U D
+            if ((st = split::gemm(sh.Xg, sh.Es, acc_m, false, derr, s))) return st;   // O E
+            col(COL_PLAIN, m, sh.Xg.expo, sh.Es.expo, sh.Fs, sh_ge);                    // F = g E + O E
+            if ((st = split::gemm(sh.Ut, sh.Fs, acc_n, false, derr, s))) return st;   // U^T F
+            col(COL_UPDATE, n, sh.Ut.expo, sh.Fs.expo, sh.Ds, sh_uf);                   // ADMM update, D
         }
         SMX_TRY_CUDA(cudaMemcpyAsync(Z_out, Z, sizeof(double) * n * B, cudaMemcpyDeviceToDevice, s));
         SMX_TRY_CUDA(cudaMemcpyAsync(dinfo + 2, derr, sizeof(int), cudaMemcpyDeviceToDevice, s));

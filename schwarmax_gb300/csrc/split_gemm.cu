@@ -144,7 +144,7 @@ struct Cfg {
     static constexpr int ACC_STRIDE = (NT + 31) / 32 * 32;
     // the exact levels' sums stay below 2^24 units over 1024 / (pairs per level) k
     static constexpr int MAXP = EXACT < (SA < SB ? SA : SB) ? EXACT : (SA < SB ? SA : SB);
-    static constexpr int CHUNK_K = MAXP <= 1 ? 1024 : MAXP == 2 ? 512 : 256;
+    static constexpr int CHUNK_K = MAXP <= 1 ? 1024 : MAXP == 2 ? 512 : MAXP <= 4 ? 256 : 128;
     static constexpr int CHUNK_KT = CHUNK_K / KT;
 };
 
@@ -154,7 +154,7 @@ __global__ void __launch_bounds__(320, 1) gemm_kernel(const GemmParams p) {
     static_assert(NT % 16 == 0 && NT <= 128 && NT >= 16, "N tile");
     static_assert(C::HALF % 8 == 0, "epilogue columns in groups of 8");
     static_assert((EXACT + 1) * C::ACC_STRIDE <= 512, "tensor memory");
-    static_assert(EXACT >= 1 && EXACT <= 4, "exact levels");
+    static_assert(EXACT >= 1 && EXACT <= 5, "exact levels");
     extern __shared__ __align__(1024) unsigned char smem[];
     uint64_t *full = (uint64_t *)(smem + STAGES * C::STAGE);
     uint64_t *empty = full + STAGES;
@@ -312,8 +312,9 @@ __global__ void __launch_bounds__(320, 1) gemm_kernel(const GemmParams p) {
                 for (int j = 0; j < 8; ++j) {
                     long long add = 0;
 #pragma unroll
-                    for (int e = 0; e < EXACT; ++e)
-                        add += (long long)__float2int_rn(v[e][j] * (float)(1 << (8 * e))) << (8 * (EXACT - 1 - e));
+                    for (int e = 0; e < EXACT; ++e)   // level 2 + e in units of 2^-8e: scale by 2^8e (exact)
+                        add += (long long)__float2int_rn(v[e][j] * __int_as_float((127 + 8 * e) << 23))
+                               << (8 * (EXACT - 1 - e));
                     sum[c0 + j] += add;
                 }
                 if (out_flush) {
@@ -474,37 +475,44 @@ static int launch_gemm(const Operand &A, const Operand &B, const Acc &acc, bool 
     return SMX_OK;
 }
 
-int exact_levels(int a_slices, int b_slices, int lmax) {
-    return (a_slices == 7 && b_slices == 7 && lmax == 8) ? 4 : 2;
+int exact_levels(const Operand &A, const Operand &B) {
+    if (A.S == 7 && B.S == 7) return 4;
+    return B.tile_rows == 64 ? 5 : 3;
 }
 
-int gemm(const Operand &A, const Operand &B, int lmax, const Acc &acc, bool lower_only, int *err, cudaStream_t s) {
+// Kernel configurations: every slice pair is formed (LMAX = SA + SB).  Column
+// tiles of 112 or 128 leave room for three exact levels (four accumulators of
+// 128 tensor-memory columns); 64-wide tiles for five (six accumulators), for
+// operands whose rows are dominated by one element (an inverse's diagonal);
+// 7 x 7 slices use pairs up to s + t = 8, four exact levels and 96-wide tiles.
+int gemm(const Operand &A, const Operand &B, const Acc &acc, bool lower_only, int *err, cudaStream_t s) {
     if (!A.slices || !A.expo || !B.slices || !B.expo || !acc.T || !acc.R || !err)
         return set_error(SMX_ERR_ARGUMENT, "split gemm: operand or accumulator without storage");
     if (acc.ld < A.rows) return set_error(SMX_ERR_ARGUMENT, "split gemm: accumulator leading dimension too small");
     if (A.k_tiles != B.k_tiles || A.tile_rows != MT)
         return set_error(SMX_ERR_ARGUMENT, "split gemm: operand shapes do not match");
     if (lower_only && B.tile_rows != MT) return set_error(SMX_ERR_ARGUMENT, "split gemm: lower_only needs square tiles");
-    const int key = A.S * 1000 + B.S * 100 + lmax * 10;
+    const int key = A.S * 10 + B.S;
     if (B.tile_rows == 112) {
         switch (key) {
-            case 4460: return launch_gemm<4, 4, 6, 112, 2>(A, B, acc, lower_only, err, s);
-            case 5460: return launch_gemm<5, 4, 6, 112, 2>(A, B, acc, lower_only, err, s);
+            case 44: return launch_gemm<4, 4, 8, 112, 3>(A, B, acc, lower_only, err, s);
+            case 45: return launch_gemm<4, 5, 9, 112, 3>(A, B, acc, lower_only, err, s);
+            case 54: return launch_gemm<5, 4, 9, 112, 3>(A, B, acc, lower_only, err, s);
+            case 55: return launch_gemm<5, 5, 10, 112, 3>(A, B, acc, lower_only, err, s);
             default: break;
         }
     } else if (B.tile_rows == 128) {
         switch (key) {
-            case 4460: return launch_gemm<4, 4, 6, 128, 2>(A, B, acc, lower_only, err, s);
-            case 5560: return launch_gemm<5, 5, 6, 128, 2>(A, B, acc, lower_only, err, s);
+            case 44: return launch_gemm<4, 4, 8, 128, 3>(A, B, acc, lower_only, err, s);
+            case 55: return launch_gemm<5, 5, 10, 128, 3>(A, B, acc, lower_only, err, s);
             default: break;
         }
     } else if (B.tile_rows == 96) {
-        switch (key) {
-            case 7780: return launch_gemm<7, 7, 8, 96, 4>(A, B, acc, lower_only, err, s);
-            default: break;
-        }
+        if (key == 77) return launch_gemm<7, 7, 8, 96, 4>(A, B, acc, lower_only, err, s);
+    } else if (B.tile_rows == 64) {
+        if (key == 55) return launch_gemm<5, 5, 10, 64, 5>(A, B, acc, lower_only, err, s);
     }
-    return set_error(SMX_ERR_UNSUPPORTED, "split gemm: no kernel for %d x %d slices, level %d, tile %d", A.S, B.S, lmax,
+    return set_error(SMX_ERR_UNSUPPORTED, "split gemm: no kernel for %d x %d slices with %d-row column tiles", A.S, B.S,
                      B.tile_rows);
 }
 
@@ -579,12 +587,12 @@ struct ProductLayout {
 };
 
 static int product_layout(int64_t M, int64_t N, int64_t K, int sa, int sb, ProductLayout *L) {
-    const bool ok44 = sa == 4 && sb == 4, ok54 = sa == 5 && sb == 4, ok55 = sa == 5 && sb == 5,
-               ok77 = sa == 7 && sb == 7;
+    const bool ab45 = (sa == 4 || sa == 5) && (sb == 4 || sb == 5), square = (sa == 4 && sb == 4) || (sa == 5 && sb == 5);
     int bt;
-    if (N <= 112 && (ok44 || ok54)) bt = 112;
-    else if (ok44 || ok55) bt = 128;
-    else if (ok77) bt = 96;
+    if (sa == 5 && sb == 5 && N <= 128) bt = 64;
+    else if (N <= 112 && ab45) bt = 112;
+    else if (square) bt = 128;
+    else if (sa == 7 && sb == 7) bt = 96;
     else return set_error(SMX_ERR_UNSUPPORTED, "smx_split_gemm: slices %d x %d with N = %lld", sa, sb, (long long)N);
     L->A = make_operand(M, K, MT, sa);
     L->B = make_operand(N, K, bt, sb);
@@ -647,9 +655,8 @@ extern "C" int smx_split_gemm(int64_t M, int64_t N, int64_t K, int a_slices, int
     if ((st = split::slice_rows<double>(A, 1, M, a, (unsigned long long *)(ws + L.rowmax), s))) return st;
     if ((st = split::slice_rows<double>(B, K, 1, b, (unsigned long long *)(ws + L.rowmax), s))) return st;
     split::Acc acc{T, R, M};
-    const int lmax = (a_slices == 7 && b_slices == 7) ? 8 : 6;
-    if ((st = split::gemm(a, b, lmax, acc, lower != 0, err, s))) return st;
-    const int shift = 8 * (split::exact_levels(a_slices, b_slices, lmax) - 1);
+    if ((st = split::gemm(a, b, acc, lower != 0, err, s))) return st;
+    const int shift = 8 * (split::exact_levels(a, b) - 1);
     split::combine_kernel<<<split::grid_for(M * N, 256), 256, 0, s>>>(T, R, a.expo, b.expo, C, M, N, shift);
     count_launch();
     SMX_TRY_CUDA(cudaGetLastError());

@@ -19,15 +19,17 @@
 //   2^24 of those units, so the FP32 accumulation is exact.  At the end of every
 //   chunk the exact levels are combined into one int64 running sum per output
 //   (units 2^-8(EXACT-1)), which is exact as well;
-//   the remaining levels share one FP32 accumulator whose rounding is 2^-24 of a
-//   term already 2^-8 EXACT below the leading one.
+//   the remaining levels share one FP32 accumulator.
+// Rows with one dominant element (the diagonal of an inverse) carry most of a
+// product in the lower levels, and the tensor cores' FP32 accumulation there
+// leaves a systematic error, so every slice pair is formed (LMAX = SA + SB)
+// with three exact levels (column tiles of 112 or 128) or five (64-wide
+// tiles); 7 x 7 products use four exact levels and pairs up to s + t = 8.
 // The result for output (i, j) is returned as the exact int64 T and a float R,
 // both accumulated with atomics over the k ranges of all CTAs, and the consumer
 // forms   C_ij = 2^(eA_i + eB_j - 14) (T_ij 2^-8(EXACT-1) + R_ij)   in double.
-// With 4 slices (31 bits) per operand, LMAX = 6 and EXACT = 2 the product error
-// is about 2^-31 of max_k |A_ik| sum_k |B_jk| + max_k |B_jk| sum_k |A_ik| plus
-// 2^-40 K max_k |A_ik| max_k |B_jk|; 7 slices, LMAX = 8 and EXACT = 4 give
-// 2^-55 and 2^-56.
+// The remaining error is the slicing of the inputs: 2^-31 (4 slices) or 2^-39
+// (5 slices) of each row's and column's largest magnitude.
 #pragma once
 
 #include <cuda_bf16.h>
@@ -78,18 +80,17 @@ struct Acc {
     int64_t ld = 0;
 };
 
-// Exact levels of the kernel used for (a_slices, b_slices, lmax): T is returned
-// in units of 2^-8(exact - 1).  4 for 7 x 7 slices with lmax 8 (about 2^-55),
-// else 2.
-int exact_levels(int a_slices, int b_slices, int lmax);
+// Exact levels of the kernel gemm() uses for A and B: T is returned in units of
+// 2^-8(exact - 1).  5 for 64-row column tiles, 4 for 7 x 7 slices, else 3.
+int exact_levels(const Operand &A, const Operand &B);
 
-// Launch C += A B^T (A: M x K, B: N x K) into acc; B.tile_rows is 112, 128
-// (4 or 5 slices, lmax 6) or 96 (7 x 7 slices, lmax 8).
+// Launch C += A B^T (A: M x K, B: N x K) into acc.  Supported: 4 or 5 slices
+// per operand with B.tile_rows 112, 4 x 4 or 5 x 5 with 128, 5 x 5 with 64,
+// 7 x 7 with 96.
 // lower_only: only output tiles with column tile <= row tile (symmetric results,
 // requires A.tile_rows == B.tile_rows).  err receives a nonzero code if a wait
 // in the kernel gave up.
-int gemm(const Operand &A, const Operand &B, int lmax, const Acc &acc, bool lower_only, int *err,
-         cudaStream_t s);
+int gemm(const Operand &A, const Operand &B, const Acc &acc, bool lower_only, int *err, cudaStream_t s);
 
 // Row scales and slices of a strided matrix: element (r, c) at src[r*sr + c*sc],
 // r < rows, c < k.  Src is float or double.  expo and slices of op must be allocated;
