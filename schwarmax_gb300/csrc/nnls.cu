@@ -32,6 +32,7 @@
 #include <cusolverDn.h>
 
 #include <cstdio>
+#include <cmath>
 #include <cstring>
 #include <vector>
 
@@ -109,7 +110,7 @@ struct Layout {
     // split path
     size_t Tacc, Racc, rowmax, err;
     size_t Ua, Ua_e, Ut, Ut_e, Xg, Xg_e, Ds, Ds_e, Es, Es_e, Fs, Fs_e;
-    size_t G7, G7_e, X7, X7_e, X5, X5_e, R5, R5_e, Gf, Xd, Rd, Ebuf, gdiag;
+    size_t G7, G7_e, X7, X7_e, X5, X5_e, R5, R5_e, Gf, Xd, Rd, Ebuf, Fbuf, gdiag, colmax;
     int lwork_s;   // float Cholesky / inverse scratch (floats)
     int64_t acc_elems;
     size_t work_bytes, host_bytes;   // device / host scratch of the factorisation and inversion
@@ -174,7 +175,9 @@ static int layout(const smx_nnls_problem *p, Layout *L, cusolverDnHandle_t solve
         L->Xd = take(m * m * sizeof(double));
         L->Rd = take(m * m * sizeof(double));
         L->Ebuf = take(m * B * sizeof(double));
+        L->Fbuf = take(m * B * sizeof(double));
         L->gdiag = take(m * sizeof(double));
+        L->colmax = take(3 * B * sizeof(unsigned long long));
     }
     L->total = off;
     return SMX_OK;
@@ -268,14 +271,20 @@ static inline unsigned grid1d(int64_t count, int bs = 256) {
 
 // ------------------------------------------------------------ split path
 
+// exact power of two 2^p as a double, |p| < 1022
+__device__ __forceinline__ double pow2(int p) { return __longlong_as_double((long long)(1023 + p) << 52); }
+
 // value of a split product: 2^(eA_r + eB_j - 14) (T 2^-t_shift + R), t_shift = 8 (exact levels - 1)
 __device__ __forceinline__ double product_value(const unsigned long long *T, const float *R, int64_t idx, int ea,
                                                 int eb, int t_shift = 16) {
-    const double v = ldexp((double)(long long)T[idx], -t_shift) + (double)R[idx];
-    return ldexp(v, ea + eb - 14);
+    const double v = (double)(long long)T[idx] * pow2(-t_shift) + (double)R[idx];
+    return v * pow2(ea + eb - 14);
 }
 
 enum { COL_INIT = 0, COL_RESID = 1, COL_PLAIN = 2, COL_UPDATE = 3 };
+
+constexpr int VS = 5;          // slices of the vector operands: 39 bits below each column's largest magnitude
+constexpr int COL_CHUNK = 1024;   // k per CTA of the column kernels
 
 struct ColArgs {
     int64_t K, n_rhs;
@@ -287,6 +296,9 @@ struct ColArgs {
     double *E;               // COL_RESID writes E, COL_PLAIN reads it (K x n_rhs)
     const double *g;         // COL_PLAIN: diagonal of G^-1, applied exactly
     double *Z, *Uu, *D;      // COL_INIT / COL_UPDATE: iterates (K x n_rhs)
+    double *V;               // the column values to slice (E, F or D)
+    unsigned long long *colmax;    // max |V| of each column, as ordered bits
+    unsigned long long *reset;     // column maxima of another operand, cleared here (n_rhs)
     const double *coefp;
     double w_init;
     __nv_bfloat16 *slices;   // output operand: n_rhs x K, VS slices, tiles of tile_rows x KT
@@ -296,23 +308,23 @@ struct ColArgs {
     int t_shift;             // units of the product's T: 2^-t_shift
 };
 
-// One CTA per right-hand side j.  Pass 1 forms the column's values (and for
-// COL_INIT / COL_UPDATE the new z, u, D = k (z - u)) and their largest
-// magnitude; pass 2 slices them into the B-operand tiles of the next product.
+// Phase 1 of a column step, grid (K / COL_CHUNK, n_rhs): forms the new column values
+// and their largest magnitude per column.
+//   COL_INIT:   z = w_init, u = 0, D = k w_init
 //   COL_RESID:  E = Y - U D                 (the residual y - U D)
 //   COL_PLAIN:  F = g E + O E               (G^-1 = diag(g) + O; O E is the product)
-//   COL_UPDATE: w = D + U^T F; w^ = 1.6 w - 0.6 z; z = max(0, w^ + u); u += w^ - z
-constexpr int VS = 5;   // slices of the vector operands: 39 bits below each column's largest magnitude
-
+//   COL_UPDATE: w = D + U^T F; w^ = 1.6 w - 0.6 z; z = max(0, w^ + u); u += w^ - z; D = k (z - u)
 template <int MODE>
-__global__ void __launch_bounds__(512) column_slice_kernel(const ColArgs a) {
-    const int64_t j = blockIdx.x, K = a.K;
-    __shared__ double red[16];
-    __shared__ int e_sh;
+__global__ void __launch_bounds__(256) column_values_kernel(const ColArgs a) {
+    const int64_t j = blockIdx.y, K = a.K;
+    if (blockIdx.x == 0 && blockIdx.y == 0)
+        for (int i = threadIdx.x; i < a.n_rhs; i += blockDim.x) a.reset[i] = 0ull;
     const int eb = (MODE == COL_INIT) ? 0 : a.eB[j];
     const double coef = a.coefp[0];
     double mx = 0;
-    for (int64_t k = threadIdx.x; k < K; k += blockDim.x) {
+    const int64_t k0 = blockIdx.x * (int64_t)COL_CHUNK;
+    const int64_t k1 = k0 + COL_CHUNK < K ? k0 + COL_CHUNK : K;
+    for (int64_t k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
         const int64_t idx = k + K * j;
         double v;
         if (MODE == COL_INIT) {
@@ -336,62 +348,57 @@ __global__ void __launch_bounds__(512) column_slice_kernel(const ColArgs a) {
             a.D[idx] = v;
         } else {
             v = product_value(a.T, a.R, idx, a.eA[k], eb, a.t_shift);
+            a.T[idx] = 0ull;
+            a.R[idx] = 0.0f;
             if (MODE == COL_RESID) {
                 v = a.Y[idx] - v;
                 a.E[idx] = v;
             } else {
                 v += a.g[k] * a.E[idx];
+                a.V[idx] = v;
             }
         }
         mx = fmax(mx, fabs(v));
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    __shared__ double red[8];
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
     __syncthreads();
     if (threadIdx.x == 0) {
         double m2 = 0;
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m2 = fmax(m2, red[w]);
-        int e = 0;
-        if (m2 > 0) frexp(m2, &e);
-        e_sh = e;
-        a.expo[j] = e;
+        atomicMax(a.colmax + j, (unsigned long long)__double_as_longlong(m2));
     }
-    __syncthreads();
-    const int e = e_sh;
+}
+
+// Phase 2, grid (K / COL_CHUNK, n_rhs), COL_CHUNK / 8 threads: the column's scale
+// 2^e > max |V| and the VS slices of every value, written as 16-byte vectors into
+// the B-operand tiles of the next product (padding k stays zero).
+__global__ void __launch_bounds__(COL_CHUNK / 8) column_slices_kernel(const ColArgs a) {
+    const int64_t j = blockIdx.y, K = a.K;
+    const double mx = __longlong_as_double((long long)a.colmax[j]);
+    int e = 0;
+    if (mx > 0) frexp(mx, &e);
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.expo[j] = e;
     const int64_t jt = j / a.tile_rows, jr = j % a.tile_rows;
-    const int64_t groups = a.k_tiles * (split::KT / 8);
-    for (int64_t g = threadIdx.x; g < groups; g += blockDim.x) {
-        __align__(16) __nv_bfloat16 sl[VS][8];
+    const int64_t g = (blockIdx.x * (int64_t)COL_CHUNK) / 8 + threadIdx.x;   // group of 8 k
+    if (g >= a.k_tiles * (split::KT / 8)) return;
+    __align__(16) __nv_bfloat16 sl[VS][8];
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            const int64_t k = g * 8 + q;
-            double v = 0;
-            if (k < K) {
-                const int64_t idx = k + K * j;
-                if (MODE == COL_INIT || MODE == COL_UPDATE) {
-                    v = a.D[idx];
-                } else {
-                    v = product_value(a.T, a.R, idx, a.eA[k], eb, a.t_shift);
-                    v = (MODE == COL_RESID) ? a.Y[idx] - v : v + a.g[k] * a.E[idx];
-                    a.T[idx] = 0ull;
-                    a.R[idx] = 0.0f;
-                }
-            }
-            double r = ldexp(v, 7 - e);
+    for (int q = 0; q < 8; ++q) {
+        const int64_t k = g * 8 + q;
+        const double v = k < K ? a.V[k + K * j] : 0.0;
+        __nv_bfloat16 d[VS];
+        split::make_slices<VS>(v, e, d);
 #pragma unroll
-            for (int s = 0; s < VS; ++s) {
-                const double ai = rint(r);
-                sl[s][q] = __float2bfloat16_rn((float)ldexp(ai, -8 * s));
-                r = (r - ai) * 256.0;
-            }
-        }
-        const int64_t k0 = g * 8, kt = k0 / split::KT;
-        const int64_t base = (jt * a.k_tiles + kt) * (int64_t)a.tile_rows * split::KT +
-                             split::tile_offset((int)jr, (int)(k0 % split::KT), a.tile_rows);
-#pragma unroll
-        for (int s = 0; s < VS; ++s) *(uint4 *)(a.slices + s * a.slice_elems + base) = *(const uint4 *)sl[s];
+        for (int s = 0; s < VS; ++s) sl[s][q] = d[s];
     }
+    const int64_t k0 = g * 8, kt = k0 / split::KT;
+    const int64_t base = (jt * a.k_tiles + kt) * (int64_t)a.tile_rows * split::KT +
+                         split::tile_offset((int)jr, (int)(k0 % split::KT), a.tile_rows);
+#pragma unroll
+    for (int s = 0; s < VS; ++s) *(uint4 *)(a.slices + s * a.slice_elems + base) = *(const uint4 *)sl[s];
 }
 
 // Gram combine: G = 2^(e_r + e_c - 14)(T/256 + R) + c I from the lower-triangle
@@ -422,23 +429,28 @@ __global__ void seed_kernel(const float *Gf, double *X, int64_t m) {
     }
 }
 
-// residual R = I - G X of a Newton-Schulz step (product with four exact levels,
-// T in units of 2^-24); rmax receives max |R| as ordered bits
-__global__ void ns_residual_kernel(unsigned long long *T, float *Racc, const int32_t *eG, const int32_t *eX, double *Rd,
-                                   int64_t m, unsigned long long *rmax) {
-    double mx = 0;
+// residual R = I - G X of a Newton-Schulz step.  G and X are dominated by their
+// diagonals, so G X = D_G X + O_G D_X + O_G O_X with D the diagonals and O the
+// rest: the first two terms are formed here in double, only O_G O_X comes from
+// the split product (four exact levels, T in units of 2^-24).  rss receives
+// sum R_ij^2 (||R||_F^2, a bound on ||R||_2^2).
+__global__ void ns_residual_kernel(unsigned long long *T, float *Racc, const int32_t *eG, const int32_t *eX,
+                                   const double *G, const double *X, double *Rd, int64_t m, double *rss) {
+    double acc = 0;
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < m * m; k += (int64_t)gridDim.x * blockDim.x) {
         const int64_t r = k % m, col = k / m;
-        const double gx = ldexp((double)(long long)T[k] * 0x1p-24 + (double)Racc[k], eG[r] + eX[col] - 14);
+        double gx = ldexp((double)(long long)T[k] * 0x1p-24 + (double)Racc[k], eG[r] + eX[col] - 14);
+        gx += G[r + m * r] * X[k];
+        if (r != col) gx += G[k] * X[col + m * col];
         const double v = (r == col ? 1.0 : 0.0) - gx;
         Rd[k] = v;
-        mx = fmax(mx, fabs(v));
+        acc += v * v;
         T[k] = 0ull;
         Racc[k] = 0.0f;
     }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    if ((threadIdx.x & 31) == 0) atomicMax(rmax, (unsigned long long)__double_as_longlong(mx));
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(rss, acc);
 }
 
 // X <- X + X R
@@ -567,44 +579,41 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
         gram_combine_kernel<<<grid1d(m * m), 256, 0, s>>>(Tacc, Racc, sh.Ua.expo, G, Gf, m, frob, lam, (double)n);
         count_launch();
         // G^-1: float Cholesky inverse as the seed, then Newton-Schulz steps
-        //   R = I - G X (7 x 7 slices, error about 2^-55 |G||X|), X <- X + X R.
-        // The new X has residual R^2, so the loop stops after the step whose
-        // input had max |R| <= 1e-6; the result is limited by the accuracy of
-        // G X times cond(G), about 2^-44.
+        //   R = I - G X (diagonals exact, off-diagonal parts as a 7 x 7 split
+        //   product), X <- X + X R.
+        // The new X has residual R^2, whose 2-norm is at most ||R||_F^2: steps
+        // continue until a step's input has ||R||_F <= 3e-7, so the result has
+        // ||I - G X|| <= 1e-13 up to the accuracy of G X times cond(G) (about 2^-44).
         SMX_TRY_SOLVER(cusolverDnSpotrf(h->solver, CUBLAS_FILL_MODE_LOWER, (int)m, Gf, (int)m, (float *)(ws + L.work),
                                         L.lwork_s, dinfo));
         SMX_TRY_SOLVER(cusolverDnSpotri(h->solver, CUBLAS_FILL_MODE_LOWER, (int)m, Gf, (int)m, (float *)(ws + L.work),
                                         L.lwork_s, dinfo + 1));
         seed_kernel<<<grid1d(m * m), 256, 0, s>>>(Gf, Xd, m);
         count_launch();
-        if ((st = split::slice_rows<double>(G, 1, m, sh.G7, rowmax, s))) return st;
-        unsigned long long *rmax = (unsigned long long *)(frob + 3);
-        double res = 1.0;
-        int steps = 0;
-        for (; steps < 6 && res > 1e-12; ++steps) {
-            if ((st = split::slice_rows<double>(Xd, m, 1, sh.X7, rowmax, s))) return st;   // X columns over k
+        if ((st = split::slice_rows<double>(G, 1, m, sh.G7, rowmax, s, true))) return st;   // O_G
+        double *rss = frob + 3;
+        double fro = 1.0;
+        for (int steps = 0; steps < 6 && fro > 3e-7; ++steps) {
+            if ((st = split::slice_rows<double>(Xd, m, 1, sh.X7, rowmax, s, true))) return st;   // O_X columns over k
             if ((st = split::gemm(sh.G7, sh.X7, acc, false, derr, s))) return st;
-            SMX_TRY_CUDA(cudaMemsetAsync(rmax, 0, sizeof(unsigned long long), s));
-            ns_residual_kernel<<<grid1d(m * m), 256, 0, s>>>(Tacc, Racc, sh.G7.expo, sh.X7.expo, Rd, m, rmax);
+            SMX_TRY_CUDA(cudaMemsetAsync(rss, 0, sizeof(double), s));
+            ns_residual_kernel<<<grid1d(m * m), 256, 0, s>>>(Tacc, Racc, sh.G7.expo, sh.X7.expo, G, Xd, Rd, m, rss);
             count_launch();
             if ((st = split::slice_rows<double>(Xd, 1, m, sh.X5, rowmax, s))) return st;   // X rows over k
             if ((st = split::slice_rows<double>(Rd, m, 1, sh.R5, rowmax, s))) return st;   // R columns over k
             if ((st = split::gemm(sh.X5, sh.R5, acc, false, derr, s))) return st;
             ns_update_kernel<<<grid1d(m * m), 256, 0, s>>>(Tacc, Racc, sh.X5.expo, sh.R5.expo, Xd, m);
             count_launch();
-            unsigned long long bits = 0;
-            SMX_TRY_CUDA(cudaMemcpyAsync(&bits, rmax, sizeof(bits), cudaMemcpyDeviceToHost, s));
+            double ss = 0;
+            SMX_TRY_CUDA(cudaMemcpyAsync(&ss, rss, sizeof(ss), cudaMemcpyDeviceToHost, s));
             SMX_TRY_CUDA(cudaStreamSynchronize(s));
-            double r;
-            memcpy(&r, &bits, sizeof(r));
-            // the residual of the step's input X: the updated X has about its square
-            res = r * r;
-            if (!(r < 0.5)) break;   // not converging: the seed is too far off
+            fro = sqrt(ss);
+            if (!(fro < 0.5)) break;   // not converging: the seed is too far off
         }
-        if (!(res <= 1e-12)) {
+        if (!(fro <= 3e-7)) {
             SMX_TRY_CUDA(cudaStreamSynchronize(s));
-            return set_error(SMX_ERR_NUMERIC, "Newton-Schulz inverse of rho' I + U U^T did not converge (residual^2 %g)",
-                             res);
+            return set_error(SMX_ERR_NUMERIC, "Newton-Schulz inverse of rho' I + U U^T did not converge (||I - G X||_F %g)",
+                             fro);
         }
         double *gdiag = (double *)(ws + L.gdiag), *Ebuf = (double *)(ws + L.Ebuf);
         split_diag_kernel<<<grid1d(m), 256, 0, s>>>(Xd, gdiag, m);
@@ -612,6 +621,11 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
         if ((st = split::slice_rows<double>(Xd, 1, m, sh.Xg, rowmax, s))) return st;   // O rows over columns
         double *Z = (double *)(ws + L.Z), *Uu = (double *)(ws + L.Uu), *D = (double *)(ws + L.D);
         const double *coefp = frob + 1;
+        // column maxima of the three vector operands (D, E, F), cleared once here and
+        // afterwards by the phase-1 kernel of the operand that follows each one
+        unsigned long long *cmD = (unsigned long long *)(ws + L.colmax), *cmE = cmD + B, *cmF = cmE + B;
+        SMX_TRY_CUDA(cudaMemsetAsync(cmD, 0, 3 * B * sizeof(unsigned long long), s));
+        double *Fbuf = (double *)(ws + L.Fbuf);
         auto col = [&](int mode, int64_t K, const int32_t *eA, const int32_t *eB, split::Operand &out,
                        int t_shift) -> int {
             ColArgs a;
@@ -635,12 +649,25 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
             a.slice_elems = out.slice_elems();
             a.tile_rows = out.tile_rows;
             a.t_shift = t_shift;
-            switch (mode) {
-                case COL_INIT: column_slice_kernel<COL_INIT><<<(unsigned)B, 512, 0, s>>>(a); break;
-                case COL_RESID: column_slice_kernel<COL_RESID><<<(unsigned)B, 512, 0, s>>>(a); break;
-                case COL_PLAIN: column_slice_kernel<COL_PLAIN><<<(unsigned)B, 512, 0, s>>>(a); break;
-                default: column_slice_kernel<COL_UPDATE><<<(unsigned)B, 512, 0, s>>>(a); break;
+            // E follows D, F follows E, D follows F
+            if (mode == COL_RESID) {
+                a.V = Ebuf; a.colmax = cmE; a.reset = cmD;
+            } else if (mode == COL_PLAIN) {
+                a.V = Fbuf; a.colmax = cmF; a.reset = cmE;
+            } else {
+                a.V = D; a.colmax = cmD; a.reset = cmF;
             }
+            const dim3 g((unsigned)((K + COL_CHUNK - 1) / COL_CHUNK), (unsigned)B);
+            switch (mode) {
+                case COL_INIT: column_values_kernel<COL_INIT><<<g, 256, 0, s>>>(a); break;
+                case COL_RESID: column_values_kernel<COL_RESID><<<g, 256, 0, s>>>(a); break;
+                case COL_PLAIN: column_values_kernel<COL_PLAIN><<<g, 256, 0, s>>>(a); break;
+                default: column_values_kernel<COL_UPDATE><<<g, 256, 0, s>>>(a); break;
+            }
+            count_launch();
+            // phase 2 covers the padded k range of the operand's tiles
+            const dim3 g2((unsigned)((out.k_tiles * split::KT + COL_CHUNK - 1) / COL_CHUNK), (unsigned)B);
+            column_slices_kernel<<<g2, COL_CHUNK / 8, 0, s>>>(a);
             count_launch();
             return SMX_OK;
         };

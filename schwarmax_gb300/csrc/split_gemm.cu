@@ -144,8 +144,8 @@ struct Cfg {
     static constexpr int ACC_STRIDE = (NT + 31) / 32 * 32;
     // the exact levels' sums stay below 2^24 units over 1024 / (pairs per level) k
     static constexpr int MAXP = EXACT < (SA < SB ? SA : SB) ? EXACT : (SA < SB ? SA : SB);
-    static constexpr int CHUNK_K = MAXP <= 1 ? 1024 : MAXP == 2 ? 512 : MAXP <= 4 ? 256 : 128;
-    static constexpr int CHUNK_KT = CHUNK_K / KT;
+    static constexpr int CHUNK_KT = (MAXP < 1 ? 1024 : 1024 / MAXP) / KT;
+    static_assert(CHUNK_KT >= 1, "chunk");
 };
 
 template <int SA, int SB, int LMAX, int NT, int EXACT, int STAGES>
@@ -222,6 +222,26 @@ __global__ void __launch_bounds__(320, 1) gemm_kernel(const GemmParams p) {
             int since_chunk = 0, since_out = 0;
             uint32_t flushes = 0;
             uint32_t fresh = (1u << (EXACT + 1)) - 1;   // accumulators to overwrite on their next MMA
+            bool pending = false;                       // a chunk flush whose read-out has not been confirmed
+            // one unit's MMAs of the exact levels (EXACTS = true) or of the rounded one
+            auto issue = [&](uint32_t sa, uint32_t sb, bool exacts) {
+#pragma unroll
+                for (int j = 0; j < KT / 16; ++j) {
+#pragma unroll
+                    for (int s = 1; s <= SA; ++s) {
+#pragma unroll
+                        for (int t = 1; t <= SB; ++t) {
+                            if (s + t <= LMAX && ((s + t - 2 < EXACT) == exacts)) {
+                                const uint64_t ad = dev::desc(sa + (s - 1) * C::A_TILE + j * 2 * LBO_A, LBO_A, SBO);
+                                const uint64_t bd = dev::desc(sb + (t - 1) * C::B_TILE + j * 2 * LBO_B, LBO_B, SBO);
+                                const int acc = (s + t - 2) < EXACT ? (s + t - 2) : EXACT;
+                                dev::mma(tmem + acc * C::ACC_STRIDE, ad, bd, ID, (fresh >> acc) & 1u ? 0u : 1u);
+                                fresh &= ~(1u << acc);
+                            }
+                        }
+                    }
+                }
+            };
             for (int64_t u = u0; u < u1; ++u, ++it) {
                 const int stage = (int)(it % STAGES);
                 if (!dev::mbar_wait(full + stage, (uint32_t)((it / STAGES) & 1), abort_flag)) {
@@ -232,22 +252,19 @@ __global__ void __launch_bounds__(320, 1) gemm_kernel(const GemmParams p) {
                 dev::fence_after();
                 const uint32_t sa = dev::smem_u32(smem + stage * C::STAGE);
                 const uint32_t sb = sa + SA * C::A_TILE;
-#pragma unroll
-                for (int j = 0; j < KT / 16; ++j) {
-#pragma unroll
-                    for (int s = 1; s <= SA; ++s) {
-#pragma unroll
-                        for (int t = 1; t <= SB; ++t) {
-                            if (s + t <= LMAX) {
-                                const uint64_t ad = dev::desc(sa + (s - 1) * C::A_TILE + j * 2 * LBO_A, LBO_A, SBO);
-                                const uint64_t bd = dev::desc(sb + (t - 1) * C::B_TILE + j * 2 * LBO_B, LBO_B, SBO);
-                                const int acc = (s + t - 2) < EXACT ? (s + t - 2) : EXACT;
-                                dev::mma(tmem + acc * C::ACC_STRIDE, ad, bd, ID, (fresh >> acc) & 1u ? 0u : 1u);
-                                fresh &= ~(1u << acc);
-                            }
-                        }
+                // the rounded level is not read at a chunk flush, so its MMAs go first
+                // while the epilogue still reads the exact levels of the previous chunk
+                issue(sa, sb, false);
+                if (pending) {
+                    if (!dev::mbar_wait(acc_empty, (flushes - 1) & 1, abort_flag)) {
+                        atomicExch(p.err, 3);
+                        *abort_flag = 1;
+                        break;
                     }
+                    dev::fence_after();
+                    pending = false;
                 }
+                issue(sa, sb, true);
                 dev::commit(empty + stage);
                 ++since_chunk;
                 ++since_out;
@@ -255,20 +272,23 @@ __global__ void __launch_bounds__(320, 1) gemm_kernel(const GemmParams p) {
                 const bool out_flush = tile_end || since_out == OUT_KT;
                 if (out_flush || since_chunk == C::CHUNK_KT) {
                     dev::commit(acc_full);
-                    if (u + 1 < u1) {
-                        if (!dev::mbar_wait(acc_empty, flushes & 1, abort_flag)) {
-                            atomicExch(p.err, 3);
-                            *abort_flag = 1;
-                            break;
-                        }
-                        dev::fence_after();
-                    }
                     ++flushes;
                     fresh |= (1u << EXACT) - 1;
                     since_chunk = 0;
                     if (out_flush) {
+                        // the rounded level is read too: wait before any further MMA
+                        if (u + 1 < u1) {
+                            if (!dev::mbar_wait(acc_empty, (flushes - 1) & 1, abort_flag)) {
+                                atomicExch(p.err, 3);
+                                *abort_flag = 1;
+                                break;
+                            }
+                            dev::fence_after();
+                        }
                         fresh |= 1u << EXACT;
                         since_out = 0;
+                    } else {
+                        pending = true;
                     }
                 }
             }
@@ -349,21 +369,23 @@ __global__ void __launch_bounds__(320, 1) gemm_kernel(const GemmParams p) {
 // max |x| per row, as the bits of a non-negative double (ordered like the values)
 template <typename T>
 __global__ void rowmax_kernel(const T *__restrict__ src, int64_t sr, int64_t sc, int64_t rows, int64_t k,
-                              unsigned long long *rowmax, int rows_fast) {
+                              unsigned long long *rowmax, int rows_fast, int skip_diag) {
     if (rows_fast) {   // consecutive threads on consecutive rows; blocks along k
         const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
         if (r >= rows) return;
         const int64_t kc = (k + gridDim.y - 1) / gridDim.y;
         const int64_t k0 = blockIdx.y * kc, k1 = k0 + kc < k ? k0 + kc : k;
         double m = 0;
-        for (int64_t c = k0; c < k1; ++c) m = fmax(m, fabs((double)src[r * sr + c * sc]));
+        for (int64_t c = k0; c < k1; ++c)
+            if (!(skip_diag && c == r)) m = fmax(m, fabs((double)src[r * sr + c * sc]));
         atomicMax(rowmax + r, (unsigned long long)__double_as_longlong(m));
     } else {           // one warp per row, lanes along k
         const int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
         const int lane = threadIdx.x & 31;
         if (r >= rows) return;
         double m = 0;
-        for (int64_t c = lane; c < k; c += 32) m = fmax(m, fabs((double)src[r * sr + c * sc]));
+        for (int64_t c = lane; c < k; c += 32)
+            if (!(skip_diag && c == r)) m = fmax(m, fabs((double)src[r * sr + c * sc]));
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
         if (lane == 0) atomicMax(rowmax + r, (unsigned long long)__double_as_longlong(m));
@@ -383,24 +405,12 @@ __global__ void expo_kernel(const unsigned long long *rowmax, int32_t *expo, int
         expo[r] = r < rows ? scale_exponent(__longlong_as_double((long long)rowmax[r])) : 0;
 }
 
-// slices of one value x < 2^e in magnitude: a'_s = a_s 2^-8(s-1), a_s in [-128, 128]
-template <int S>
-__device__ __forceinline__ void make_slices(double x, int e, __nv_bfloat16 *out) {
-    double r = ldexp(x, 7 - e);
-#pragma unroll
-    for (int s = 0; s < S; ++s) {
-        const double a = rint(r);
-        out[s] = __float2bfloat16_rn((float)ldexp(a, -8 * s));
-        r = (r - a) * 256.0;
-    }
-}
-
 // one CTA per (row tile, k tile): builds the S slice tiles in shared memory and
 // writes each as contiguous 16-byte vectors
 template <typename T, int S>
 __global__ void slice_rows_kernel(const T *__restrict__ src, int64_t sr, int64_t sc, int64_t rows, int64_t k,
                                   const int32_t *__restrict__ expo, __nv_bfloat16 *slices, int tile_rows,
-                                  int64_t k_tiles, int64_t slice_elems, int k_fast) {
+                                  int64_t k_tiles, int64_t slice_elems, int k_fast, int skip_diag) {
     extern __shared__ __align__(16) unsigned char sm_raw[];
     __nv_bfloat16 *tile = (__nv_bfloat16 *)sm_raw;   // S x tile_rows x KT
     const int64_t kt = blockIdx.x, rt = blockIdx.y;
@@ -417,7 +427,7 @@ __global__ void slice_rows_kernel(const T *__restrict__ src, int64_t sr, int64_t
         const int64_t gr = rt * tile_rows + r, gc = kt * KT + c;
         double x = 0;
         int e = 0;
-        if (gr < rows && gc < k) {
+        if (gr < rows && gc < k && !(skip_diag && gr == gc)) {
             x = (double)src[gr * sr + gc * sc];
             e = expo[gr];
         }
@@ -523,7 +533,8 @@ static inline unsigned grid_for(int64_t count, int bs) {
 }
 
 template <typename T>
-int slice_rows(const T *src, int64_t sr, int64_t sc, const Operand &op, unsigned long long *rowmax, cudaStream_t s) {
+int slice_rows(const T *src, int64_t sr, int64_t sc, const Operand &op, unsigned long long *rowmax, cudaStream_t s,
+               bool skip_diag) {
     if (!src || !op.slices || !op.expo || !rowmax)
         return set_error(SMX_ERR_ARGUMENT, "slice_rows: operand without storage");
     const int64_t rows_padded = op.row_tiles * op.tile_rows;
@@ -532,9 +543,10 @@ int slice_rows(const T *src, int64_t sr, int64_t sc, const Operand &op, unsigned
     const bool rows_fast = sr == 1;
     if (rows_fast) {
         dim3 g((unsigned)((op.rows + 255) / 256), (unsigned)(op.k < 64 ? op.k : 64));
-        rowmax_kernel<T><<<g, 256, 0, s>>>(src, sr, sc, op.rows, op.k, rowmax, 1);
+        rowmax_kernel<T><<<g, 256, 0, s>>>(src, sr, sc, op.rows, op.k, rowmax, 1, skip_diag ? 1 : 0);
     } else {
-        rowmax_kernel<T><<<grid_for(op.rows * 32, 256), 256, 0, s>>>(src, sr, sc, op.rows, op.k, rowmax, 0);
+        rowmax_kernel<T><<<grid_for(op.rows * 32, 256), 256, 0, s>>>(src, sr, sc, op.rows, op.k, rowmax, 0,
+                                                                   skip_diag ? 1 : 0);
     }
     count_launch();
     expo_kernel<<<grid_for(rows_padded, 256), 256, 0, s>>>(rowmax, op.expo, op.rows, rows_padded);
@@ -548,7 +560,7 @@ int slice_rows(const T *src, int64_t sr, int64_t sc, const Operand &op, unsigned
         SMX_TRY_CUDA(cudaFuncSetAttribute(slice_rows_kernel<T, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
                                           (int)sm));                                                             \
         slice_rows_kernel<T, NS><<<g, 256, sm, s>>>(src, sr, sc, op.rows, op.k, op.expo, op.slices, op.tile_rows,  \
-                                                    op.k_tiles, op.slice_elems(), k_fast);                       \
+                                                    op.k_tiles, op.slice_elems(), k_fast, skip_diag ? 1 : 0);    \
         break;
         SMX_SLICE_CASE(4)
         SMX_SLICE_CASE(5)
@@ -561,8 +573,10 @@ int slice_rows(const T *src, int64_t sr, int64_t sc, const Operand &op, unsigned
     return SMX_OK;
 }
 
-template int slice_rows<float>(const float *, int64_t, int64_t, const Operand &, unsigned long long *, cudaStream_t);
-template int slice_rows<double>(const double *, int64_t, int64_t, const Operand &, unsigned long long *, cudaStream_t);
+template int slice_rows<float>(const float *, int64_t, int64_t, const Operand &, unsigned long long *, cudaStream_t,
+                               bool);
+template int slice_rows<double>(const double *, int64_t, int64_t, const Operand &, unsigned long long *, cudaStream_t,
+                                bool);
 
 }  // namespace split
 }  // namespace smx

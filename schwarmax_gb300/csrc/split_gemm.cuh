@@ -49,6 +49,52 @@ __host__ __device__ inline int64_t tile_offset(int r, int k, int rows) {
     return ((int64_t)((k >> 3) * (rows >> 3) + (r >> 3)) << 6) + ((r & 7) << 3) + (k & 7);
 }
 
+// round(x 2^k) as an integer, from the bits of x (round half to even; |result|
+// must stay below 2^62).  Integer arithmetic only: GB300's FP64 rate is low.
+__device__ __forceinline__ long long to_fixed(double x, int k) {
+    const long long b = __double_as_longlong(x);
+    const int E = (int)((b >> 52) & 0x7FF);
+    if (E == 0) return 0;                               // zero (and subnormals, < 2^-1022)
+    const long long m = (b & ((1LL << 52) - 1)) | (1LL << 52);
+    const int sh = E - 1075 + k;                        // x 2^k = m 2^sh
+    long long v;
+    if (sh >= 0) {
+        v = m << sh;
+    } else if (sh < -54) {
+        v = 0;
+    } else {
+        const int r = -sh;
+        const long long q = m >> r, rem = m & ((1LL << r) - 1), half = 1LL << (r - 1);
+        v = q + ((rem > half || (rem == half && (q & 1))) ? 1 : 0);
+    }
+    return b < 0 ? -v : v;
+}
+__device__ __forceinline__ long long to_fixed(float x, int k) { return to_fixed((double)x, k); }
+
+// S slices of a value already scaled to a signed integer v, |v| <= 2^(7 + 8(S-1)):
+// balanced base-256 digits a_s in [-128, 128], v = sum a_s 256^(S-1-s), stored as
+// bf16 a_s 2^-8s (exact).
+template <int S>
+__device__ __forceinline__ void digits(long long v, __nv_bfloat16 *out) {
+#pragma unroll
+    for (int s = S - 1; s > 0; --s) {
+        int d = (int)(v & 0xFF);
+        v >>= 8;                                        // arithmetic shift: floor division
+        if (d > 128) {
+            d -= 256;
+            v += 1;
+        }
+        out[s] = __float2bfloat16_rn(__int_as_float((127 - 8 * s) << 23) * (float)d);
+    }
+    out[0] = __float2bfloat16_rn((float)v);
+}
+
+// slices of x with scale exponent e (|x| < 2^e): x 2^(7 + 8(S-1) - e) rounded
+template <int S, typename T>
+__device__ __forceinline__ void make_slices(T x, int e, __nv_bfloat16 *out) {
+    digits<S>(to_fixed(x, 7 + 8 * (S - 1) - e), out);
+}
+
 // Sliced operand: rows x k values as S bf16 slices in K-major tiles of
 // tile_rows x KT, tiles ordered [slice][row tile][k tile]; expo[row] = e.
 struct Operand {
@@ -94,10 +140,11 @@ int gemm(const Operand &A, const Operand &B, const Acc &acc, bool lower_only, in
 
 // Row scales and slices of a strided matrix: element (r, c) at src[r*sr + c*sc],
 // r < rows, c < k.  Src is float or double.  expo and slices of op must be allocated;
-// slices padded with zeros.  rowmax is scratch of rows uint64.
+// slices padded with zeros.  rowmax is scratch of rows uint64.  skip_diag: the
+// entries r == c are taken as 0 (the off-diagonal part of a square matrix).
 template <typename T>
 int slice_rows(const T *src, int64_t sr, int64_t sc, const Operand &op, unsigned long long *rowmax,
-               cudaStream_t s);
+               cudaStream_t s, bool skip_diag = false);
 
 }  // namespace split
 }  // namespace smx
