@@ -213,7 +213,7 @@ def run_ours(args, rank, world, local):
     if rank == 0:
         line = {"metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3), "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f32 (orbits, binning) / tf32+f64 (NNLS)",
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32 (orbits, binning) / bf16 split products + f64 (NNLS)",
                 "data": "synthetic (seeded; schwarmax_gb300.synthetic)",
                 "config": {"workload": WORKLOAD, "parallelism": f"replicas x{world}",
                            "l2": "working set > L2 (no flush)", "setup_s": round(setup_s, 1)},

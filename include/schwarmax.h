@@ -121,6 +121,13 @@ typedef struct {
     int64_t max_attempts;  /* sampled mode: cap per orbit (status bit 1 when hit) */
     double atol, rtol, dt_min, dt_max;
     double omega;          /* frame angular velocity Omega = -Omega_bar (kpc/Gyr) */
+    const int32_t *order;  /* optional (NULL = 0, 1, 2, ...): device array of n_orb orbit
+                              indices, the order in which the work queue hands orbits out.
+                              Orbits sorted by expected cost, longest first, keep the
+                              lanes of a warp busy for similar times.  Results do not
+                              depend on it.  Entries outside [0, n_orb) are skipped; an
+                              orbit missing from it is not integrated.  No counterpart in
+                              the reference. */
 } smx_integrator;
 
 /* Per-orbit record written by smx_integrate (array of n_orb, precision of the

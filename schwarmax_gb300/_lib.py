@@ -94,7 +94,7 @@ class SmxIntegrator(ctypes.Structure):
     _fields_ = [("mode", ctypes.c_int), ("store_all", ctypes.c_int), ("n_attempts", ctypes.c_int),
                 ("n_samples", ctypes.c_int), ("max_attempts", ctypes.c_int64), ("atol", ctypes.c_double),
                 ("rtol", ctypes.c_double), ("dt_min", ctypes.c_double), ("dt_max", ctypes.c_double),
-                ("omega", ctypes.c_double)]
+                ("omega", ctypes.c_double), ("order", ctypes.c_void_p)]
 
 
 class SmxBinning(ctypes.Structure):

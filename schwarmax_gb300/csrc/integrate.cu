@@ -19,6 +19,7 @@ template <typename T> struct IntegT {
     T atol, rtol, dt_min, dt_max, om;
     int mode, store_all, n_attempts, n_samples;
     long long max_attempts;
+    const int32_t *order;   // queue position -> orbit (NULL: identity)
 };
 
 template <typename T>
@@ -98,7 +99,17 @@ __global__ void __launch_bounds__(128) integrate_kernel(PotT<T> P, IntegT<T> I, 
     for (int c = 0; c < 6; ++c) k2[c] = k3[c] = k4[c] = yn[c] = T(0);
     T dt = T(0), t = T(0), h = T(0), wsum = T(0);
     int att = 0, n_acc = 0, next = 0, flags = 0;
-    int orb = atomicAdd(queue, 1);
+    // q: position in the work queue; orb: the orbit at that position (entries of
+    // order outside [0, n_orb) are skipped, so a bad permutation cannot write
+    // out of bounds)
+    int q, orb = 0;
+    auto take = [&]() {
+        do {
+            q = atomicAdd(queue, 1);
+            orb = q < n_orb ? (I.order ? I.order[q] : q) : 0;
+        } while (q < n_orb && (orb < 0 || orb >= n_orb));
+    };
+    take();
 
     auto load = [&](int o) {
         const T *base = samples + (int64_t)o * slots;
@@ -113,9 +124,9 @@ __global__ void __launch_bounds__(128) integrate_kernel(PotT<T> P, IntegT<T> I, 
         h = sampled ? t_end[o] / T(n_samp) : T(0);
         att = n_acc = next = flags = 0;
     };
-    if (orb < n_orb) load(orb);
+    if (q < n_orb) load(orb);
 
-    while (orb < n_orb) {
+    while (q < n_orb) {
         ++att;
         // stage inputs are formed as soon as their slopes exist, so the stage loop
         // body is one force evaluation plus a uniform branch on s
@@ -231,8 +242,8 @@ __global__ void __launch_bounds__(128) integrate_kernel(PotT<T> P, IntegT<T> I, 
             info[SMX_INFO_NACC * n_orb + orb] = T(n_acc);
             info[SMX_INFO_NATT * n_orb + orb] = T(att);
             status[orb] = flags;
-            orb = atomicAdd(queue, 1);
-            if (orb < n_orb) load(orb);
+            take();
+            if (q < n_orb) load(orb);
         }
     }
 }
@@ -252,6 +263,7 @@ static int launch(const smx_potential *pot, const smx_integrator *cfg, const voi
     I.n_attempts = cfg->n_attempts;
     I.n_samples = cfg->n_samples;
     I.max_attempts = cfg->max_attempts;
+    I.order = cfg->order;
     SMX_TRY_CUDA(cudaMemsetAsync(queue, 0, sizeof(int32_t), s));
     integrate_init_kernel<T><<<(unsigned)((n_orb + 127) / 128), 128, 0, s>>>(make_pot<T>(*pot), T(cfg->omega),
                                                                          (const T *)w0, n_orb, slots,
@@ -263,9 +275,13 @@ static int launch(const smx_potential *pot, const smx_integrator *cfg, const voi
     int per_sm = 0;
     SMX_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, integrate_kernel<T>, 128, 0));
     if (per_sm < 1) per_sm = 1;
-    int64_t blocks = (n_orb + 127) / 128;
-    const int64_t resident = (int64_t)sms * per_sm;
-    if (blocks > resident) blocks = resident;
+    // the same number of blocks on every SM: orbits come from the queue, so every
+    // SM keeps working until the queue is empty (512 blocks for 65,536 orbits
+    // would put 4 blocks on some SMs and 3 on others)
+    int64_t bps = (n_orb + (int64_t)sms * 128 - 1) / ((int64_t)sms * 128);
+    if (bps > per_sm) bps = per_sm;
+    int64_t blocks = (int64_t)sms * bps;
+    if (blocks > (n_orb + 127) / 128 * 2 && (n_orb + 127) / 128 < sms) blocks = (n_orb + 127) / 128;   // tiny calls
     integrate_kernel<T><<<(unsigned)blocks, 128, 0, s>>>(make_pot<T>(*pot), I, (const T *)w0, (const T *)dt_init,
                                                          (const T *)t_total, n_orb, slots, (T *)samples, n_stored,
                                                          (T *)info, status, queue);

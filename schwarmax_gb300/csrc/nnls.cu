@@ -672,16 +672,18 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
             return SMX_OK;
         };
         split::Acc acc_m{Tacc, Racc, m}, acc_n{Tacc, Racc, n};
+        // U D and U^T F drop the slice pairs s + t >= 8 (U has no dominant
+        // element per row or column: its products sit in the exact levels)
         const int sh_ud = 8 * (split::exact_levels(sh.Ua, sh.Ds) - 1);
         const int sh_ge = 8 * (split::exact_levels(sh.Xg, sh.Es) - 1);
         const int sh_uf = 8 * (split::exact_levels(sh.Ut, sh.Fs) - 1);
         col(COL_INIT, n, nullptr, nullptr, sh.Ds, 0);
         for (int it = 0; it < p->maxiter; ++it) {
-            if ((st = split::gemm(sh.Ua, sh.Ds, acc_m, false, derr, s))) return st;   // U D
+            if ((st = split::gemm(sh.Ua, sh.Ds, acc_m, false, derr, s, 7))) return st;   // U D
             col(COL_RESID, m, sh.Ua.expo, sh.Ds.expo, sh.Es, sh_ud);                    // E = Y - U D
             if ((st = split::gemm(sh.Xg, sh.Es, acc_m, false, derr, s))) return st;   // O E
             col(COL_PLAIN, m, sh.Xg.expo, sh.Es.expo, sh.Fs, sh_ge);                    // F = g E + O E
-            if ((st = split::gemm(sh.Ut, sh.Fs, acc_n, false, derr, s))) return st;   // U^T F
+            if ((st = split::gemm(sh.Ut, sh.Fs, acc_n, false, derr, s, 7))) return st;   // U^T F
             col(COL_UPDATE, n, sh.Ut.expo, sh.Fs.expo, sh.Ds, sh_uf);                   // ADMM update, D
         }
         SMX_TRY_CUDA(cudaMemcpyAsync(Z_out, Z, sizeof(double) * n * B, cudaMemcpyDeviceToDevice, s));

@@ -495,7 +495,7 @@ int exact_levels(const Operand &A, const Operand &B) {
 // 128 tensor-memory columns); 64-wide tiles for five (six accumulators), for
 // operands whose rows are dominated by one element (an inverse's diagonal);
 // 7 x 7 slices use pairs up to s + t = 8, four exact levels and 96-wide tiles.
-int gemm(const Operand &A, const Operand &B, const Acc &acc, bool lower_only, int *err, cudaStream_t s) {
+int gemm(const Operand &A, const Operand &B, const Acc &acc, bool lower_only, int *err, cudaStream_t s, int lmax) {
     if (!A.slices || !A.expo || !B.slices || !B.expo || !acc.T || !acc.R || !err)
         return set_error(SMX_ERR_ARGUMENT, "split gemm: operand or accumulator without storage");
     if (acc.ld < A.rows) return set_error(SMX_ERR_ARGUMENT, "split gemm: accumulator leading dimension too small");
@@ -503,6 +503,9 @@ int gemm(const Operand &A, const Operand &B, const Acc &acc, bool lower_only, in
         return set_error(SMX_ERR_ARGUMENT, "split gemm: operand shapes do not match");
     if (lower_only && B.tile_rows != MT) return set_error(SMX_ERR_ARGUMENT, "split gemm: lower_only needs square tiles");
     const int key = A.S * 10 + B.S;
+    if (B.tile_rows == 112 && key == 45 && lmax == 7)
+        return launch_gemm<4, 5, 7, 112, 3>(A, B, acc, lower_only, err, s);
+    if (lmax != 0) return set_error(SMX_ERR_UNSUPPORTED, "split gemm: no kernel with pairs up to s + t = %d", lmax);
     if (B.tile_rows == 112) {
         switch (key) {
             case 44: return launch_gemm<4, 4, 8, 112, 3>(A, B, acc, lower_only, err, s);

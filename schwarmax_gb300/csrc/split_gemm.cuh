@@ -136,7 +136,10 @@ int exact_levels(const Operand &A, const Operand &B);
 // lower_only: only output tiles with column tile <= row tile (symmetric results,
 // requires A.tile_rows == B.tile_rows).  err receives a nonzero code if a wait
 // in the kernel gave up.
-int gemm(const Operand &A, const Operand &B, const Acc &acc, bool lower_only, int *err, cudaStream_t s);
+// lmax = 0 forms every slice pair; lmax = 7 (4 x 5 slices, 112-wide tiles) drops
+// the pairs s + t >= 8, about 2^-47 of max|A| max|B| per product term.
+int gemm(const Operand &A, const Operand &B, const Acc &acc, bool lower_only, int *err, cudaStream_t s,
+         int lmax = 0);
 
 // Row scales and slices of a strided matrix: element (r, c) at src[r*sr + c*sc],
 // r < rows, c < k.  Src is float or double.  expo and slices of op must be allocated;

@@ -18,7 +18,7 @@ import numpy as np
 import torch
 
 from . import kernels
-from ._lib import SMX_MODE_REFERENCE, SMX_MODE_SAMPLED, SmxBinning, SmxIntegrator
+from ._lib import INFO_NATT, SMX_MODE_REFERENCE, SMX_MODE_SAMPLED, SmxBinning, SmxIntegrator
 from .potentials import potential_struct
 
 EPSILON = 1e-12
@@ -41,7 +41,8 @@ class Settings:
     n_samples: int = 1000
     max_attempts: int = 1_000_000
     bulge_mass: float = None
-    precision: str = "mixed"         # "mixed" (FP32 orbits, TF32/FP64 NNLS) or "fp64"
+    precision: str = "mixed"         # "mixed" (FP32 orbits, split tensor-core NNLS) or "fp64"
+    order_probe: bool = False        # sampled mode: order the orbits by the cost of a one-period probe
 
     @property
     def dtype(self):
@@ -161,14 +162,31 @@ class Grid:
 _buffers = {}
 
 
-def _integrator_buffers(n_orb, slots, dtype):
-    key = (n_orb, slots, dtype)
+def _integrator_buffers(n_orb, slots, dtype, role="main"):
+    key = (role, n_orb, slots, dtype)
     b = _buffers.get(key)
     if b is None:
-        _buffers.clear()
+        for k in [k for k in _buffers if k[0] == role]:
+            del _buffers[k]
         b = kernels.IntegratorBuffers(n_orb, slots, dtype, torch.device("cuda"))
         _buffers[key] = b
     return b
+
+
+def probe_order(pot, cfg, ic, st: Settings):
+    """Orbit order for the sampled integration, longest first: attempts of each
+    orbit over one circular period (1/n_periods of its horizon).  The order
+    changes which lanes share a warp, not any result."""
+    frac = 1.0 / max(st.n_periods, 1.0)
+    ns = max(1, int(round(st.n_samples * frac)))
+    pcfg = SmxIntegrator(mode=SMX_MODE_SAMPLED, store_all=0, n_attempts=0, n_samples=ns,
+                         max_attempts=max(1, int(st.max_attempts * frac)), atol=cfg.atol, rtol=cfg.rtol,
+                         dt_min=cfg.dt_min, dt_max=cfg.dt_max, omega=cfg.omega)
+    n_orb = ic["w0"].shape[1]
+    pb = _integrator_buffers(n_orb, ns, st.dtype, role="probe")
+    kernels.integrate(pot, pcfg, ic["w0"], ic["dt_init"], (ic["t_total"] * frac).contiguous(), pb)
+    cost = pb.info[INFO_NATT]
+    return torch.argsort(cost, descending=True).to(torch.int32).contiguous()
 
 
 def build_library(pot, params_disk_rho, dd: DeviceData, grid: Grid, st: Settings, trajectory=False):
@@ -185,6 +203,10 @@ def build_library(pot, params_disk_rho, dd: DeviceData, grid: Grid, st: Settings
                         max_attempts=st.max_attempts, atol=st.atol, rtol=st.rtol, dt_min=st.dt_min,
                         dt_max=st.dt_max, omega=-float(params_disk_rho["Omega_bar"]))
     slots = st.n_attempts if mode == "reference" else st.n_samples
+    order = None
+    if mode == "sampled" and st.order_probe:
+        order = probe_order(pot, cfg, ic, st)
+        cfg.order = order.data_ptr()
     bufs = _integrator_buffers(dd.n * n_real, slots, dtype)
     kernels.integrate(pot, cfg, ic["w0"], ic["dt_init"], ic["t_total"], bufs)
     geo = binning_geometry(params_disk_rho, grid, dd, n_real, symmetry=0 if trajectory else 1)
