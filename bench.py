@@ -210,6 +210,9 @@ def run_ours(args, rank, world, local):
     cpu = None
     if rank == 0 and world == 1 and not args.skip_cpu:
         cpu = cpu_baseline(cfg, quick=True)
+    adj = None
+    if rank == 0 and args.adjoint:
+        adj = adjoint_timing(dict_data, theta, cfg, st)
     if rank == 0:
         line = {"metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3), "higher_is_better": True,
@@ -219,6 +222,8 @@ def run_ours(args, rank, world, local):
                            "l2": "working set > L2 (no flush)", "setup_s": round(setup_s, 1)},
                 "gpu_launches": int(launches), "roofline": roofline, "stages_ms": stages, "precision": prec, "e2e": e2e,
                 "cpu_baseline": cpu, "clocks": clocks, "logL_last": float(val.item())}
+        if adj is not None:
+            line["adjoint"] = adj
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -457,6 +462,39 @@ def run_reference(args, rank, world):
     print(json.dumps(line))
 
 
+def adjoint_timing(dict_data, theta, cfg, st):
+    """Config 3: the chi^2 gradient with respect to (alpha, beta, gamma, velocity
+    scale) on this evaluation's stored orbits (soft apertures, sigma 0.5 pixel),
+    timed after one warm-up gradient; one component checked by central
+    differences (step 1e-4 rad)."""
+    import numpy as np
+    import torch
+
+    from schwarmax_gb300 import adjoint
+    prob, th0 = adjoint.problem_from_evaluation(theta, dict_data, cfg.n_bins,
+                                                cfg.n_grid[0] * cfg.n_grid[1] * cfg.n_grid[2], settings=st,
+                                                sigma_pix=0.5, precision="mixed")
+    th = th0 + np.array([0.05, -0.05, 0.05, 0.05])
+    prob.chi2_and_grad(th)
+    torch.cuda.synchronize()
+    t0 = time.time()
+    tim = {}
+    c2, g = prob.chi2_and_grad(th, timings=tim)
+    torch.cuda.synchronize()
+    t_grad = time.time() - t0
+    fd = {}
+    for hstep in (1e-4, 1e-5):
+        e = np.array([hstep, 0.0, 0.0, 0.0])
+        fd[str(hstep)] = (prob.chi2(th + e) - prob.chi2(th - e)) / (2 * hstep)
+    g = g.cpu().numpy()
+    return {"workload": "config3: soft apertures (sigma 0.5 px) on the config-1 stored orbits, single data row, "
+                        "FP64 soft projection, ADMM + active-set KKT NNLS",
+            "s_per_gradient": round(t_grad, 3), "stages_s": {k: (round(v, 3) if isinstance(v, float) else v)
+                                                             for k, v in tim.items()},
+            "chi2": c2, "grad_alpha_beta_gamma_vscale": [float(v) for v in g],
+            "fd_alpha": fd, "fd_rel_err_alpha": {k: float(abs(g[0] - v) / max(abs(v), 1e-300)) for k, v in fd.items()}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -469,6 +507,8 @@ def main():
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--adjoint", action="store_true",
+                    help="also time the chi^2 gradient of the differentiable projection + NNLS on this library")
     ap.add_argument("--out", default=os.path.join(ROOT, "gpurun_out"))
     args = ap.parse_args()
     args.config = int(args.config) if args.config.isdigit() else args.config

@@ -212,6 +212,29 @@ int smx_project_bin(const smx_binning *geo, int precision, const void *samples,
 int smx_sample_cells(const smx_binning *geo, int precision, const void *points, int64_t n,
                      const int32_t *bin_mapping, int32_t *cells, int32_t *bins, void *vlos, void *stream);
 
+/* ------------------------------------------------- differentiable projection */
+/* Sky rows [xy | h0..h4] of the library (rows n_cells .. n_cells + 6 n_bins of each
+ * particle's column, same normalisation and validity as smx_project_bin) with soft
+ * aperture assignment: each sample image is spread over the pixels by a Gaussian of
+ * sigma_pix pixels integrated over each pixel (window +-3 pixels), and its
+ * line-of-sight velocity is multiplied by vscale.  geo->rot is the rotation for the
+ * viewing angles.  The Rzphi rows are not written.  No reference counterpart (the
+ * reference has no gradient: stop_gradient at nnls.py:66,165). */
+int smx_soft_project(const smx_binning *geo, int precision, double sigma_pix, double vscale, const void *samples,
+                     const int32_t *n_stored, int64_t slots, const void *info, const void *t_total,
+                     const int32_t *bin_mapping, const double *num_per_bin, const double *v0, const double *s,
+                     void *library, void *stream);
+
+/* Adjoint of smx_soft_project: grad[0..3] += dL/d(alpha, beta, gamma, vscale) for a
+ * cotangent dL/dlibrary (n_part, rows) of the call's precision (only the sky rows are
+ * read).  drot (3 x 9 doubles, host memory, like geo->rot) holds d rot / d alpha,
+ * d beta, d gamma.  The rotated samples are recomputed, not stored. */
+int smx_soft_project_adjoint(const smx_binning *geo, int precision, double sigma_pix, double vscale,
+                             const double *drot, const void *samples, const int32_t *n_stored, int64_t slots,
+                             const void *info, const void *t_total, const int32_t *bin_mapping,
+                             const double *num_per_bin, const double *v0, const double *s, const void *cotangent,
+                             double *grad, void *stream);
+
 /* ------------------------------------------------------------------- NNLS */
 enum { SMX_NNLS_FP64 = 0, SMX_NNLS_MIXED = 1 };
 

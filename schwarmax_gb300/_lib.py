@@ -18,7 +18,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(HERE, "libschwarmax_gb300.so")
-SOURCES = ["api.cu", "pointkernels.cu", "integrate.cu", "project_bin.cu", "nnls.cu", "split_gemm.cu", "maps.cu"]
+SOURCES = ["api.cu", "pointkernels.cu", "integrate.cu", "project_bin.cu", "soft_project.cu", "nnls.cu", "split_gemm.cu",
+           "maps.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 SMX_FP32, SMX_FP64 = 0, 1
@@ -28,7 +29,8 @@ INFO_T, INFO_EJ0, INFO_EJ, INFO_WSUM, INFO_NACC, INFO_NATT, INFO_FIELDS = range(
 
 EXPORTS = ["smx_version", "smx_kernel_launches", "smx_status_string", "smx_last_error", "smx_potential_eval",
            "smx_initial_conditions", "smx_density_target", "smx_integrate", "smx_integrate_noalloc", "smx_project_bin",
-           "smx_sample_cells", "smx_nnls_workspace_size", "smx_nnls_admm", "smx_split_gemm_workspace_size",
+           "smx_sample_cells", "smx_soft_project", "smx_soft_project_adjoint", "smx_nnls_workspace_size",
+           "smx_nnls_admm", "smx_split_gemm_workspace_size",
            "smx_split_gemm", "smx_model_maps", "smx_model_maps_workspace_size"]
 
 
@@ -139,6 +141,10 @@ _SIGS = {
     "smx_project_bin": ([ctypes.POINTER(SmxBinning), ctypes.c_int, _P, _P, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _P],
                         ctypes.c_int),
     "smx_sample_cells": ([ctypes.POINTER(SmxBinning), ctypes.c_int, _P, _I64, _P, _P, _P, _P, _P], ctypes.c_int),
+    "smx_soft_project": ([ctypes.POINTER(SmxBinning), ctypes.c_int, ctypes.c_double, ctypes.c_double, _P, _P,
+                          ctypes.c_int64, _P, _P, _P, _P, _P, _P, _P, _P], ctypes.c_int),
+    "smx_soft_project_adjoint": ([ctypes.POINTER(SmxBinning), ctypes.c_int, ctypes.c_double, ctypes.c_double, _P, _P,
+                                  _P, ctypes.c_int64, _P, _P, _P, _P, _P, _P, _P, _P, _P], ctypes.c_int),
     "smx_nnls_workspace_size": ([ctypes.POINTER(SmxNnlsProblem), ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
     "smx_nnls_admm": ([ctypes.POINTER(SmxNnlsProblem), _P, _P, _P, _P, _P, _P, ctypes.c_size_t, _P], ctypes.c_int),
     "smx_split_gemm_workspace_size": ([ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int, ctypes.c_int,
