@@ -218,8 +218,10 @@ int smx_sample_cells(const smx_binning *geo, int precision, const void *points, 
  * aperture assignment: each sample image is spread over the pixels by a Gaussian of
  * sigma_pix pixels integrated over each pixel (window +-3 pixels), and its
  * line-of-sight velocity is multiplied by vscale.  geo->rot is the rotation for the
- * viewing angles.  The Rzphi rows are not written.  No reference counterpart (the
- * reference has no gradient: stop_gradient at nnls.py:66,165). */
+ * viewing angles.  The Rzphi rows are not written.  In double the sums are exact
+ * fixed-point sums (units of 2^-56, so the rows are deterministic); they hold for
+ * finite dispersions s >= 0.01 km/s, which keep every row sum below 64.  No reference
+ * counterpart (the reference has no gradient: stop_gradient at nnls.py:66,165). */
 int smx_soft_project(const smx_binning *geo, int precision, double sigma_pix, double vscale, const void *samples,
                      const int32_t *n_stored, int64_t slots, const void *info, const void *t_total,
                      const int32_t *bin_mapping, const double *num_per_bin, const double *v0, const double *s,

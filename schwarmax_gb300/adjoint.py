@@ -90,6 +90,9 @@ class SoftProblem:
         self.amp = float(sigma_amplify)
         self.lam = float(regularization)
         self.admm_iters = int(admm_iters)
+        s_min = float(dd.s.min())
+        if not (math.isfinite(s_min) and s_min >= 0.01):
+            raise ValueError(f"soft projection needs finite dispersions >= 0.01 km/s, got min {s_min}")
         self.h_data = dd.h.double()                # (4, nb) observed h1..h4 (bootstrap 0)
         self.sig_h = (dd.h_err + engine.EPSILON).double()
 

@@ -141,17 +141,25 @@ __device__ __forceinline__ void hermite(T y, T (&H)[5]) {
     H[4] = (sq2 * y * H[3] - sq3 * H[2]) * T(0.5);
 }
 
-// forward: one CTA per particle, sky rows accumulated in shared memory
+// forward: one CTA per particle, the sky rows of the library accumulated with
+// global reductions (red_add).  In double they are exact int64 fixed-point sums
+// in units of 2^-56 (every row sum stays below 64), stored in place of the
+// doubles and converted after, so the rows do not depend on the order of the
+// adds.  Float rows take float adds.  Separate kernels zero the rows before and
+// convert / normalise them after.
+__device__ __forceinline__ void add(float *p, float v) { red_add(p, v); }
+__device__ __forceinline__ void add(double *p, double v) {
+    red_add(reinterpret_cast<unsigned long long *>(p), (unsigned long long)__double2ll_rn(v * 0x1p56));
+}
+
 template <typename T>
-__global__ void __launch_bounds__(256) soft_project_kernel(Geo<T> G, SoftArgs a, T *library) {
-    extern __shared__ unsigned char smem_raw[];
-    T *acc = reinterpret_cast<T *>(smem_raw);   // 6 n_bins
+__global__ void __launch_bounds__(256, 1) soft_project_kernel(Geo<T> G, SoftArgs a, T *library) {
     __shared__ double scale_r[8];
     const int p = blockIdx.x;
     const int nbins = G.n_bins;
-    for (int i = threadIdx.x; i < 6 * nbins; i += blockDim.x) acc[i] = T(0);
     if (threadIdx.x == 0) realisation_scales(G, a, p, scale_r);
     __syncthreads();
+    T *acc = library + (int64_t)p * G.rows + G.n_cells;   // [xy | h0..h4] of this particle
     const T *samples = (const T *)a.samples;
     const int64_t n_orb = (int64_t)G.n_part * G.n_real;
     const int64_t cs = n_orb * a.slots;
@@ -185,19 +193,33 @@ __global__ void __launch_bounds__(256) soft_project_kernel(Geo<T> G, SoftArgs a,
                     const T gw = w * Wb * isq2pi / sb * exp(T(-0.5) * yv * yv);
                     T H[5];
                     hermite(yv, H);
-                    atomicAdd(&acc[b], w * Wb);
+                    add(&acc[b], w * Wb);
 #pragma unroll
-                    for (int k = 0; k < 5; ++k) atomicAdd(&acc[(1 + k) * nbins + b], gw * H[k]);
+                    for (int k = 0; k < 5; ++k) add(&acc[(1 + k) * nbins + b], gw * H[k]);
                 });
             }
         }
     }
-    __syncthreads();
-    T *col = library + (int64_t)p * G.rows + G.n_cells;
-    for (int i = threadIdx.x; i < 6 * nbins; i += blockDim.x) {
-        T v = acc[i];
-        if (i < nbins) v = T((double)v / (a.num_per_bin[i] * a.area + kEps));
-        col[i] = v;
+}
+
+// sky rows of every particle: zero (mode 0), or (mode 1) convert the fixed-point
+// sums of double rows and divide the xy row by num_per_bin x area
+template <typename T>
+__global__ void sky_rows_kernel(T *library, int64_t n_part, int rows, int n_cells, int nbins,
+                                const double *__restrict__ num_per_bin, double area, int mode) {
+    const int64_t per = 6 * (int64_t)nbins;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n_part * per;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t p = k / per, i = k % per;
+        T *v = library + p * rows + n_cells + i;
+        if (mode == 0) {
+            *v = T(0);   // also int64 0 in double rows
+        } else {
+            double x = (double)*v;
+            if (sizeof(T) == 8) x = (double)*reinterpret_cast<const long long *>(v) * 0x1p-56;
+            if (i < nbins) x /= num_per_bin[i] * area + kEps;
+            *v = T(x);
+        }
     }
 }
 
@@ -349,22 +371,28 @@ extern "C" int smx_soft_project(const smx_binning *geo, int precision, double si
     soft::SoftArgs a{samples, n_stored, slots, info, t_total, bin_mapping, num_per_bin, v0, s,
                      ((geo->X_hi - geo->X_lo) / geo->nX) * ((geo->Y_hi - geo->Y_lo) / geo->nY) * 1e6};
     cudaStream_t sm = (cudaStream_t)stream;
+    const int rows = geo->nR * geo->nz * geo->nphi + 6 * geo->n_bins;
+    const int n_cells = geo->nR * geo->nz * geo->nphi;
+    const int64_t cnt = (int64_t)geo->n_part * 6 * geo->n_bins;
+    const unsigned g1 = (unsigned)((cnt + 255) / 256 < 152 * 64 ? (cnt + 255) / 256 : 152 * 64);
     if (precision == SMX_FP32) {
-        const size_t smem = (size_t)6 * geo->n_bins * sizeof(float);
-        SMX_TRY_CUDA(cudaFuncSetAttribute(soft::soft_project_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)smem));
-        soft::soft_project_kernel<float><<<geo->n_part, 256, smem, sm>>>(soft::make<float>(geo, sigma_pix, vscale, nullptr),
-                                                                         a, (float *)library);
+        soft::sky_rows_kernel<float><<<g1, 256, 0, sm>>>((float *)library, geo->n_part, rows, n_cells, geo->n_bins,
+                                                          num_per_bin, a.area, 0);
+        soft::soft_project_kernel<float><<<geo->n_part, 256, 0, sm>>>(soft::make<float>(geo, sigma_pix, vscale, nullptr),
+                                                                      a, (float *)library);
+        soft::sky_rows_kernel<float><<<g1, 256, 0, sm>>>((float *)library, geo->n_part, rows, n_cells, geo->n_bins,
+                                                          num_per_bin, a.area, 1);
     } else if (precision == SMX_FP64) {
-        const size_t smem = (size_t)6 * geo->n_bins * sizeof(double);
-        SMX_TRY_CUDA(cudaFuncSetAttribute(soft::soft_project_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)smem));
-        soft::soft_project_kernel<double><<<geo->n_part, 256, smem, sm>>>(
+        soft::sky_rows_kernel<double><<<g1, 256, 0, sm>>>((double *)library, geo->n_part, rows, n_cells, geo->n_bins,
+                                                           num_per_bin, a.area, 0);
+        soft::soft_project_kernel<double><<<geo->n_part, 256, 0, sm>>>(
             soft::make<double>(geo, sigma_pix, vscale, nullptr), a, (double *)library);
+        soft::sky_rows_kernel<double><<<g1, 256, 0, sm>>>((double *)library, geo->n_part, rows, n_cells, geo->n_bins,
+                                                           num_per_bin, a.area, 1);
     } else {
         return set_error(SMX_ERR_ARGUMENT, "bad precision %d", precision);
     }
-    count_launch();
+    count_launch(3);
     SMX_TRY_CUDA(cudaGetLastError());
     return SMX_OK;
 }
