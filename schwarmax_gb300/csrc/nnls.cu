@@ -275,10 +275,13 @@ static inline unsigned grid1d(int64_t count, int bs = 256) {
 __device__ __forceinline__ double pow2(int p) { return __longlong_as_double((long long)(1023 + p) << 52); }
 
 // value of a split product: 2^(eA_r + eB_j - 14) (T 2^-t_shift + R), t_shift = 8 (exact levels - 1)
+__device__ __forceinline__ double product_of(long long t, float r, int ea, int eb, int t_shift) {
+    const double v = (double)t * pow2(-t_shift) + (double)r;
+    return v * pow2(ea + eb - 14);
+}
 __device__ __forceinline__ double product_value(const unsigned long long *T, const float *R, int64_t idx, int ea,
                                                 int eb, int t_shift = 16) {
-    const double v = (double)(long long)T[idx] * pow2(-t_shift) + (double)R[idx];
-    return v * pow2(ea + eb - 14);
+    return product_of((long long)T[idx], R[idx], ea, eb, t_shift);
 }
 
 enum { COL_INIT = 0, COL_RESID = 1, COL_PLAIN = 2, COL_UPDATE = 3 };
@@ -316,45 +319,72 @@ struct ColArgs {
 //   COL_UPDATE: w = D + U^T F; w^ = 1.6 w - 0.6 z; z = max(0, w^ + u); u += w^ - z; D = k (z - u)
 template <int MODE>
 __global__ void __launch_bounds__(256) column_values_kernel(const ColArgs a) {
+    constexpr int PER = COL_CHUNK / 256;   // values per thread
     const int64_t j = blockIdx.y, K = a.K;
     if (blockIdx.x == 0 && blockIdx.y == 0)
         for (int i = threadIdx.x; i < a.n_rhs; i += blockDim.x) a.reset[i] = 0ull;
     const int eb = (MODE == COL_INIT) ? 0 : a.eB[j];
     const double coef = a.coefp[0];
+    const int64_t kb = blockIdx.x * (int64_t)COL_CHUNK;
+    const int64_t k1 = kb + COL_CHUNK < K ? kb + COL_CHUNK : K;
+    // every load of the thread's PER values is issued before any store, so that
+    // their latencies overlap (one value after another, each waited on its loads)
+    long long t[PER];
+    float r[PER];
+    int ea[PER];
+    double x[PER], y[PER], uu[PER];
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+        const int64_t k = kb + threadIdx.x + q * 256, idx = k + K * j;
+        if (k >= k1) continue;
+        if (MODE != COL_INIT) {
+            t[q] = (long long)a.T[idx];
+            r[q] = a.R[idx];
+            ea[q] = a.eA[k];
+        }
+        if (MODE == COL_UPDATE) {
+            x[q] = a.D[idx];
+            y[q] = a.Z[idx];
+            uu[q] = a.Uu[idx];
+        } else if (MODE == COL_RESID) {
+            x[q] = a.Y[idx];
+        } else if (MODE == COL_PLAIN) {
+            x[q] = a.E[idx];
+            y[q] = a.g[k];
+        }
+    }
     double mx = 0;
-    const int64_t k0 = blockIdx.x * (int64_t)COL_CHUNK;
-    const int64_t k1 = k0 + COL_CHUNK < K ? k0 + COL_CHUNK : K;
-    for (int64_t k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
-        const int64_t idx = k + K * j;
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+        const int64_t k = kb + threadIdx.x + q * 256, idx = k + K * j;
+        if (k >= k1) continue;
         double v;
         if (MODE == COL_INIT) {
             a.Z[idx] = a.w_init;
             a.Uu[idx] = 0.0;
             v = coef * a.w_init;
             a.D[idx] = v;
-        } else if (MODE == COL_UPDATE) {
-            const double gt = product_value(a.T, a.R, idx, a.eA[k], eb, a.t_shift);
-            a.T[idx] = 0ull;
-            a.R[idx] = 0.0f;
-            const double z = a.Z[idx], u = a.Uu[idx];
-            const double w = a.D[idx] + gt;
-            const double wh = 1.6 * w - 0.6 * z;
-            double zn = wh + u;
-            zn = zn > 0.0 ? zn : 0.0;
-            const double un = u + wh - zn;
-            a.Z[idx] = zn;
-            a.Uu[idx] = un;
-            v = coef * (zn - un);
-            a.D[idx] = v;
         } else {
-            v = product_value(a.T, a.R, idx, a.eA[k], eb, a.t_shift);
+            const double pv = product_of(t[q], r[q], ea[q], eb, a.t_shift);
             a.T[idx] = 0ull;
             a.R[idx] = 0.0f;
-            if (MODE == COL_RESID) {
-                v = a.Y[idx] - v;
+            if (MODE == COL_UPDATE) {
+                const double z = y[q], u = uu[q];
+                const double w = x[q] + pv;
+                const double wh = 1.6 * w - 0.6 * z;
+                double zn = wh + u;
+                zn = zn > 0.0 ? zn : 0.0;
+                const double un = u + wh - zn;
+                a.Z[idx] = zn;
+                a.Uu[idx] = un;
+                v = coef * (zn - un);
+                a.D[idx] = v;
+            } else if (MODE == COL_RESID) {
+                v = x[q] - pv;
                 a.E[idx] = v;
             } else {
-                v += a.g[k] * a.E[idx];
+                v = pv;
+                v += y[q] * x[q];
                 a.V[idx] = v;
             }
         }
