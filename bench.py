@@ -524,7 +524,7 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--adjoint", action="store_true",
                     help="also time the chi^2 gradient of the differentiable projection + NNLS on this library")
-    ap.add_argument("--out", default=os.path.join(ROOT, "gpurun_out"))
+    ap.add_argument("--out", default=os.path.join(ROOT, "bench_out"), help="folder for the clock samples")
     args = ap.parse_args()
     args.config = int(args.config) if args.config.isdigit() else args.config
     os.makedirs(args.out, exist_ok=True)

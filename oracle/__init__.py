@@ -4,7 +4,7 @@ TEST INFRASTRUCTURE ONLY.  This package is a plain NumPy (float64, with a
 float32 mode for the integer binning arithmetic) restatement of the
 reference's algorithm.  Only ``tests/``, ``__graft_entry__.smoke()`` and the
 ``cpu_baseline`` / ``--impl reference`` legs of ``bench.py`` may import it, and
-only as the checker or as the timed CPU baseline.  The product package
+only to check results or as the timed CPU baseline.  The product package
 ``schwarmax_gb300`` never imports it and has no CPU fallback.
 
 Parity pin: the restatement is checked against golden vectors produced by the

@@ -1,6 +1,6 @@
 """Dense FP64 PyTorch reference of the differentiable projection + NNLS chi^2.
 
-Test infrastructure only (tests/ import it as the checker of
+Test infrastructure only (tests/ import it to check
 smx_soft_project, smx_soft_project_adjoint and schwarmax_gb300.adjoint).  The
 reference has no such path (it stops gradients at its NNLS, nnls.py:66,165);
 what this restates is the hard binning of integrates.py:115-174 with each
