@@ -56,3 +56,70 @@ def test_argument_errors_without_gpu():
     assert st == 1
     st = lib.smx_potential_eval(ctypes.byref(pot), 7, None, None, None, 0, None, None, None, None, None, None)
     assert st == 0   # n = 0 is a no-op
+
+
+def _geo(**kw):
+    from schwarmax_gb300 import _lib
+    g = _lib.SmxBinning(n_part=5, n_real=4, nR=4, nz=3, nphi=2, R_lo=0.0, R_hi=10.0, z_lo=-3.0, z_hi=3.0,
+                        phi_lo=-3.14159, phi_hi=3.14159, nX=8, nY=8, X_lo=-1.0, X_hi=1.0, Y_lo=-1.0, Y_hi=1.0,
+                        n_bins=5, symmetry=1)
+    for k, v in kw.items():
+        setattr(g, k, v)
+    return g
+
+
+def test_soft_projection_argument_errors_without_gpu():
+    """smx_soft_project / _adjoint check sizes, sigma, the velocity scale and their
+    buffers before any device call."""
+    from schwarmax_gb300 import _lib
+    if not os.path.exists(_lib.LIB_PATH):
+        pytest.skip("library not built")
+    lib = _lib.load()
+    fake = ctypes.c_void_p(256)          # never dereferenced: every case below returns first
+
+    def proj(geo, sigma=0.5, vscale=1.0, bufs=fake):
+        return lib.smx_soft_project(geo if geo is None else ctypes.byref(geo), 1, sigma, vscale, bufs, bufs, 10,
+                                    bufs, bufs, bufs, bufs, bufs, bufs, bufs, None)
+
+    assert proj(None) == 1
+    assert proj(_geo(n_real=9)) == 1                  # realisations 1..8
+    assert proj(_geo(nX=0)) == 1
+    assert proj(_geo(X_hi=-1.0)) == 1                 # empty sky grid
+    assert proj(_geo(), sigma=0.01) == 1              # window of +-3 pixels needs sigma in [0.05, 1]
+    assert proj(_geo(), sigma=1.5) == 1
+    assert proj(_geo(), vscale=0.0) == 1
+    assert "velocity scale" in _lib.last_error()
+    assert proj(_geo(n_part=0)) == 0                  # nothing to do
+    assert proj(_geo(), bufs=None) == 1               # buffers missing
+    assert lib.smx_soft_project(ctypes.byref(_geo()), 9, 0.5, 1.0, fake, fake, 10, fake, fake, fake, fake, fake,
+                                fake, fake, None) == 1     # precision
+    drot = (ctypes.c_double * 27)()
+    grad = fake
+
+    def adj(geo, d=drot, g=grad):
+        return lib.smx_soft_project_adjoint(ctypes.byref(geo), 1, 0.5, 1.0, d, fake, fake, 10, fake, fake, fake,
+                                            fake, fake, fake, fake, g, None)
+
+    assert adj(_geo(), d=None) == 1
+    assert adj(_geo(), g=None) == 1
+    assert adj(_geo(n_part=0)) == 0
+
+
+def test_split_product_argument_errors_without_gpu():
+    from schwarmax_gb300 import _lib
+    if not os.path.exists(_lib.LIB_PATH):
+        pytest.skip("library not built")
+    lib = _lib.load()
+    nbytes = ctypes.c_size_t(0)
+    assert lib.smx_split_gemm_workspace_size(300, 100, 1000, 4, 5, ctypes.byref(nbytes)) == 0
+    need = nbytes.value
+    assert need >= 300 * 100 * 12                    # int64 + float accumulator per output at least
+    assert lib.smx_split_gemm_workspace_size(0, 100, 1000, 4, 5, ctypes.byref(nbytes)) == 1
+    assert lib.smx_split_gemm_workspace_size(300, 100, 1000, 4, 5, None) == 1
+    assert lib.smx_split_gemm_workspace_size(300, 100, 1000, 3, 3, ctypes.byref(nbytes)) == 2   # no 3-slice kernel
+    assert lib.smx_split_gemm_workspace_size(300, 200, 1000, 4, 5, ctypes.byref(nbytes)) == 2   # 4 x 5 needs N <= 112
+    fake = ctypes.c_void_p(256)
+    assert lib.smx_split_gemm(300, 100, 1000, 4, 5, 0, fake, fake, fake, fake, need - 1, None) == 6   # workspace
+    assert lib.smx_split_gemm(300, 100, 1000, 4, 5, 0, None, fake, fake, fake, need, None) == 1
+    assert lib.smx_split_gemm(300, 200, 1000, 4, 4, 1, fake, fake, fake, fake, 1 << 40, None) == 1    # lower: M == N
+    assert lib.smx_split_gemm(1 << 17, 1 << 15, 64, 4, 4, 0, fake, fake, fake, fake, 1 << 40, None) == 2  # too large
