@@ -123,3 +123,35 @@ def test_split_product_argument_errors_without_gpu():
     assert lib.smx_split_gemm(300, 100, 1000, 4, 5, 0, None, fake, fake, fake, need, None) == 1
     assert lib.smx_split_gemm(300, 200, 1000, 4, 4, 1, fake, fake, fake, fake, 1 << 40, None) == 1    # lower: M == N
     assert lib.smx_split_gemm(1 << 17, 1 << 15, 64, 4, 4, 0, fake, fake, fake, fake, 1 << 40, None) == 2  # too large
+
+
+def test_nnls_argument_errors_without_gpu():
+    """smx_nnls_admm checks the problem and its buffers before creating any handle."""
+    from schwarmax_gb300 import _lib
+    if not os.path.exists(_lib.LIB_PATH):
+        pytest.skip("library not built")
+    lib = _lib.load()
+    fake = ctypes.c_void_p(256)
+
+    def prob(**kw):
+        p = _lib.SmxNnlsProblem(n=100, m=60, n_rhs=4, ld_lib=80, lib_precision=_lib.SMX_FP32,
+                                mode=_lib.SMX_NNLS_MIXED, maxiter=10, lambda_reg=1.0, w_init=0.1)
+        for k, v in kw.items():
+            setattr(p, k, v)
+        return p
+
+    def run(p, bufs=fake):
+        return lib.smx_nnls_admm(None if p is None else ctypes.byref(p), bufs, bufs, bufs, bufs, bufs, bufs, 1 << 40,
+                                 None)
+
+    assert run(None) == 1
+    assert run(prob(n=0)) == 1
+    assert run(prob(n_rhs=0)) == 1
+    assert run(prob(maxiter=-1)) == 1
+    assert run(prob(m=50000)) == 2                    # G = c I + U U^T would exceed 2^31 entries
+    assert run(prob(mode=7)) == 1
+    assert run(prob(), bufs=None) == 1
+    assert run(prob(lambda_reg=-1.0)) == 1
+    nbytes = ctypes.c_size_t(0)
+    assert lib.smx_nnls_workspace_size(None, ctypes.byref(nbytes)) == 1
+    assert lib.smx_nnls_workspace_size(ctypes.byref(prob(m=0)), ctypes.byref(nbytes)) == 1
