@@ -123,7 +123,7 @@ static int layout(const smx_nnls_problem *p, Layout *L, cusolverDnHandle_t solve
     size_t off = 0;
     auto take = [&](size_t bytes) { size_t o = off; off = align256(off + bytes); return o; };
     *L = Layout();
-    L->U = take(m * n * (mixed ? sizeof(float) : sizeof(double)));
+    L->U = take(m * n * sizeof(double));   // U = library x row scale in double for both modes
     L->G = take(m * m * sizeof(double));
     int lwork = 0, lw_f = 0, lw_i = 0;
     if (solver) {
@@ -558,10 +558,13 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
         }
         SMX_TRY_CUDA(cudaMemcpyAsync(Z_out, Z, sizeof(double) * n * B, cudaMemcpyDeviceToDevice, s));
     } else {
-        float *U = (float *)(ws + L.U);
-        build_u_kernel<TL, float><<<gb, 256, 0, s>>>(lib, p->ld_lib, row_map, row_scale, m, n, U, dinfo + 3);
+        // U in double: rounding library x row scale to float (2^-24 of every entry, and
+        // |U|_F^2 and rho with it) moved the bootstrap chi^2 by up to 0.1 at config 1;
+        // the slices below keep 31 bits of each row's largest entry
+        double *U = (double *)(ws + L.U);
+        build_u_kernel<TL, double><<<gb, 256, 0, s>>>(lib, p->ld_lib, row_map, row_scale, m, n, U, dinfo + 3);
         count_launch();
-        frob_kernel<float><<<grid1d(m * n), 256, 0, s>>>(U, m * n, frob);
+        frob_kernel<double><<<grid1d(m * n), 256, 0, s>>>(U, m * n, frob);
         count_launch();
         admm_coef_kernel<<<1, 1, 0, s>>>(frob, lam, (double)n, frob + 1);
         count_launch();
@@ -599,8 +602,8 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
         SMX_TRY_CUDA(cudaMemsetAsync(sh.Fs.slices, 0, sh.Fs.slice_bytes(), s));
         int st;
         // U split both ways: rows of U over orbits (U D, U U^T) and orbits over rows (U^T F)
-        if ((st = split::slice_rows<float>(U, 1, m, sh.Ua, rowmax, s))) return st;
-        if ((st = split::slice_rows<float>(U, m, 1, sh.Ut, rowmax, s))) return st;
+        if ((st = split::slice_rows<double>(U, 1, m, sh.Ua, rowmax, s))) return st;
+        if ((st = split::slice_rows<double>(U, m, 1, sh.Ut, rowmax, s))) return st;
         // G = U U^T + c I, exact to about 2^-39 of the float design matrix
         split::Acc acc{Tacc, Racc, m};
         float *Gf = (float *)(ws + L.Gf);
