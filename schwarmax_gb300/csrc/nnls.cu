@@ -604,7 +604,7 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
         // U split both ways: rows of U over orbits (U D, U U^T) and orbits over rows (U^T F)
         if ((st = split::slice_rows<double>(U, 1, m, sh.Ua, rowmax, s))) return st;
         if ((st = split::slice_rows<double>(U, m, 1, sh.Ut, rowmax, s))) return st;
-        // G = U U^T + c I, exact to about 2^-39 of the float design matrix
+        // G = U U^T + c I from the sliced U (31 bits below each row's largest entry), all slice pairs
         split::Acc acc{Tacc, Racc, m};
         float *Gf = (float *)(ws + L.Gf);
         double *Xd = (double *)(ws + L.Xd), *Rd = (double *)(ws + L.Rd);
