@@ -337,9 +337,32 @@ def case_with_orbit():
                                                      "surface_density", "h1", "h2", "h3", "h4", "V", "sigma")})
 
 
+def case_example_data():
+    """The reference's loader (utils.py:572-743) on the example galaxy of its
+    checkout (example/mock_Nbody_galaxy_beta65_gamma45_D50.pkl: 609 Voronoi
+    apertures on a 60 x 40 pixel map).  Saved: the pickle's arrays as inputs
+    (in_*), and the loader's outputs (out_*) with the first two rows of each
+    bootstrap draw; the threefry-drawn w0 is left out (the device path draws its
+    own)."""
+    import pickle
+    name = "mock_Nbody_galaxy_beta65_gamma45_D50.pkl"
+    path = os.path.join(REF, "example") + os.sep
+    with open(path + name, "rb") as f:
+        raw = pickle.load(f)               # jax arrays come back as NumPy through the shim
+    d = utils.load_data_bootstrap(path, name)
+    out = {}
+    for k, v in d.items():
+        a = np.asarray(v)
+        if k == "w0":
+            continue
+        out["out_" + k] = a[:2] if k.endswith("_standard_normal") else a
+    save("example_data", **{"in_" + k: np.asarray(v) for k, v in raw.items()}, **out)
+
+
 if __name__ == "__main__":
     print("G =", constants.G, "KPCGYR_TO_KMS =", constants.KPCGYR_TO_KMS)
-    cases = sys.argv[2:] or ["potential", "small_funcs", "jeans", "integrate", "nnls", "end_to_end", "with_orbit"]
+    cases = sys.argv[2:] or ["potential", "small_funcs", "jeans", "integrate", "nnls", "end_to_end", "with_orbit",
+                             "example_data"]
     for c in cases:
         print("case", c)
         globals()["case_" + c]()
