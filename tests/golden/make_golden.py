@@ -359,6 +359,41 @@ def case_example_data():
     save("example_data", **{"in_" + k: np.asarray(v) for k, v in raw.items()}, **out)
 
 
+def case_example_end_to_end():
+    """model_likelihood and build_model on the example galaxy's apertures and grids
+    (609 bins on 60 x 40 pixels, 10 x 6 x 10 cells), with the loader's n_samples = 2
+    particles and N_BOOTSTRAP = 3, at the example's viewing angles (25, 65, 45 deg)."""
+    name = "mock_Nbody_galaxy_beta65_gamma45_D50.pkl"
+    d = utils.load_data_bootstrap(os.path.join(REF, "example") + os.sep, name, N_BOOTSTRAP=3, n_samples=2)
+    nb, nc = int(d["total_bins"]), int(d["Rzphi_n_tot"])
+    theta = np.array([10.76, 10.83, 10.2, math.log10(7.76), math.log10(3.0), math.log10(0.3),
+                      math.log10(4.0), 25 * math.pi / 180, 65 * math.pi / 180, 45 * math.pi / 180,
+                      0.05, math.log10(35.79)])
+    jax.random.DRAWS.clear()
+    t0 = time.time()
+    logl = float(likelihood.model_likelihood(theta, d, nb, nc, sigma_amplify=1.3))
+    print(f"  model_likelihood: {time.time() - t0:.1f}s  logL={logl}")
+    normals = np.stack([x[2] for x in jax.random.DRAWS if x[0] == "normal"][:3])
+    unif = np.stack([x[2] for x in jax.random.DRAWS if x[0] == "uniform"][:6])
+    halo = likelihood.logMenc_logc_to_logM_logRs(theta[0], theta[3], r_enc=10.0, Delta=200., rho_crit=277.54)
+    pb = dict(logM_disc=theta[1], Rs_disc=10 ** theta[4], Hs_disc=10 ** theta[5], logM_bar=theta[2],
+              L_bar=10 ** theta[6], a_bar=10 ** theta[6] / 5, b_bar=10 ** theta[5],
+              mass_to_light_ratio=10 ** theta[10], Omega_bar=10 ** theta[11], x_origin=0.0, y_origin=0.0,
+              z_origin=0.0, dirx=0.0, diry=0.0, dirz=1.0, alpha=theta[7] * 180 / math.pi,
+              beta=theta[8] * 180 / math.pi, gamma=theta[9] * 180 / math.pi)
+    phh = dict(logM=halo[0], Rs=10 ** halo[1], a=1.0, b=1.0, c=1.0, x_origin=0.0, y_origin=0.0,
+               z_origin=0.0, dirx=0.0, diry=0.0, dirz=1.0)
+    t0 = time.time()
+    md = model.build_model(likelihood.density_func, likelihood.potential_func, phh, pb, d, nb, nc,
+                           np.asarray(d["Rzphi_n_grid"]), np.array([d["R_minmax"], d["z_minmax"], d["phi_minmax"]]),
+                           np.array([d["X_minmax"], d["Y_minmax"]]), np.asarray(d["nX_nY"]), nnls_maxiter=60)
+    print(f"  build_model: {time.time() - t0:.1f}s")
+    arrays = {"dd_" + k: np.asarray(v) for k, v in d.items()}
+    arrays.update({"bm_" + k: np.asarray(v) for k, v in md.items()})
+    save("example_end_to_end", theta=theta, logL=np.array(logl), sigma_amplify=np.array(1.3), jeans_normals=normals,
+         jitter_uniforms=unif, **arrays)
+
+
 if __name__ == "__main__":
     print("G =", constants.G, "KPCGYR_TO_KMS =", constants.KPCGYR_TO_KMS)
     cases = sys.argv[2:] or ["potential", "small_funcs", "jeans", "integrate", "nnls", "end_to_end", "with_orbit",
