@@ -17,8 +17,6 @@ is the exact gradient of the same expression (the reference uses jax.grad).
 """
 import math
 
-import numpy as np
-
 from . import dual as D
 from .constants import G, EPSILON
 

@@ -30,7 +30,7 @@ import numpy as np
 import torch
 
 from . import engine, kernels
-from ._lib import SMX_FP32, SMX_FP64, call
+from ._lib import SMX_FP64, call
 
 KMS = 0.9777922216807892
 

@@ -12,14 +12,13 @@ Random draws are inputs: dict_data may carry 'jeans_normals' (3, n) and
 once from NumPy generators seeded with the same numbers.
 """
 import math
-from dataclasses import dataclass, field, replace
+from dataclasses import dataclass, replace
 
 import numpy as np
 import torch
 
 from . import kernels
 from ._lib import INFO_NATT, SMX_MODE_REFERENCE, SMX_MODE_SAMPLED, SmxBinning, SmxIntegrator
-from .potentials import potential_struct
 
 EPSILON = 1e-12
 KPCGYR_TO_KMS = 0.9777922216807892

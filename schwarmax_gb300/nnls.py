@@ -4,8 +4,6 @@ The A blocks are (rows, n_orb) as in the reference; they are packed into an
 orbit-major library (n_orb, rows) and solved by ``smx_nnls_admm`` (Woodbury
 form, Cholesky of the rows x rows system).  ``mixed=False`` is the FP64 path.
 """
-import math
-
 import torch
 
 from . import kernels

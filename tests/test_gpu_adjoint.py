@@ -3,8 +3,6 @@ gradients at its NNLS): the soft-aperture kernel and its adjoint against the den
 FP64 PyTorch reference in oracle/soft_projection.py, and the chi^2 gradient with
 respect to (alpha, beta, gamma, velocity scale) against central finite differences
 (step 1e-4 rad / 1e-4 relative) and against autograd of the dense reference."""
-import math
-
 import numpy as np
 import pytest
 import torch
