@@ -394,6 +394,20 @@ def case_example_end_to_end():
          jitter_uniforms=unif, **arrays)
 
 
+def case_example_jackknife():
+    """calculate_delta_chi2 (leave-one-bin-out over the 609 apertures) on the
+    example_end_to_end data and parameters, with the same draws."""
+    g = np.load(os.path.join(OUT, "example_end_to_end.npz"))
+    d = {k[3:]: g[k] for k in g.files if k.startswith("dd_")}
+    d["total_bins"] = int(d["total_bins"])
+    d["Rzphi_n_tot"] = int(d["Rzphi_n_tot"])
+    jax.random.DRAWS.clear()
+    t0 = time.time()
+    dchi2 = float(likelihood.calculate_delta_chi2(g["theta"], d, d["total_bins"], d["Rzphi_n_tot"]))
+    print(f"  calculate_delta_chi2: {time.time() - t0:.1f}s  dchi2={dchi2}")
+    save("example_jackknife", theta=g["theta"], delta_chi2=np.array(dchi2))
+
+
 if __name__ == "__main__":
     print("G =", constants.G, "KPCGYR_TO_KMS =", constants.KPCGYR_TO_KMS)
     cases = sys.argv[2:] or ["potential", "small_funcs", "jeans", "integrate", "nnls", "end_to_end", "with_orbit",

@@ -195,3 +195,16 @@ def test_end_to_end_on_the_example_galaxy():
         assert np.median(dev) <= 1e-6, k
         assert np.quantile(dev, 0.99) <= 1e-4, k
         assert np.unique(np.nonzero(dev > 1e-4)[-1]).size <= 8, k      # apertures touched by edge samples
+
+
+@pytest.mark.slow
+def test_jackknife_on_the_example_galaxy():
+    """calculate_delta_chi2 (leave-one-bin-out over 609 apertures, likelihood.py:248-336)
+    on the example galaxy, as the reference computed it.  The few samples on pixel
+    edges (see above) move it by about 1e-5."""
+    g = golden("example_end_to_end")
+    j = golden("example_jackknife")
+    dd = _tiny_dd(g)
+    d = likelihood.calculate_delta_chi2(j["theta"], dd, dd["total_bins"], dd["Rzphi_n_tot"])
+    ref = float(j["delta_chi2"])
+    assert abs(d - ref) <= 1e-4 * abs(ref), (d, ref)
