@@ -56,6 +56,13 @@ typedef struct {
     double bulge_M, bulge_a, bulge_b, bulge_L, bulge_gamma;   /* V4 */
 } smx_potential;
 
+/* One parameter point of a batched call: its potential and the frame's angular
+ * velocity Omega = -Omega_bar (kpc/Gyr). */
+typedef struct {
+    smx_potential pot;
+    double omega;
+} smx_point;
+
 /* Library version (major*10000 + minor*100 + patch). */
 int smx_version(void);
 const char *smx_status_string(int status);
@@ -150,7 +157,9 @@ enum { SMX_INFO_T = 0, SMX_INFO_EJ0 = 1, SMX_INFO_EJ = 2, SMX_INFO_WSUM = 3,
  *                              dt = dt_min was rejected, so (the step being
  *                              deterministic) all later attempts would be too and
  *                              the orbit stops there (0 = clean)
- *   queue    one int32 of device scratch (the call zeroes it). */
+ *   queue    one int32 of device scratch (the call zeroes it).
+ * n_orb <= 2^31 - 2^24 (the work counter is 32-bit); larger sizes return
+ * SMX_ERR_UNSUPPORTED. */
 int smx_integrate(const smx_potential *pot, const smx_integrator *cfg, int precision,
                   const void *w0, const void *dt_init, const void *t_total, int64_t n_orb,
                   int64_t slots, void *samples, int32_t *n_stored, void *info, int32_t *status,
@@ -165,11 +174,28 @@ int smx_integrate(const smx_potential *pot, const smx_integrator *cfg, int preci
  * SMX_ERR_UNSUPPORTED); the first call on each device looks up the array's
  * address (make it before any stream capture); calls share the counter, which
  * each call zeroes on its stream, so calls that overlap on the GPU race and
- * must be serialised by the caller.  Allocates nothing. */
+ * must be serialised by the caller.  The device address of the array is looked
+ * up once per device and kept: after cudaDeviceReset it is stale, so a process
+ * that resets a device must not call this entry point on it again.  Allocates
+ * nothing. */
 int smx_integrate_noalloc(const smx_potential *pot, const smx_integrator *cfg, int precision,
                           const void *w0, const void *dt_init, const void *t_total, int64_t n_orb,
                           int64_t slots, void *samples, int32_t *n_stored, void *info, int32_t *status,
                           void *stream);
+
+/* The orbits of n_points parameter points in one launch with one work queue
+ * (the batched evaluation of jax.vmap(model_likelihood) over parameter points,
+ * example/example_schwarmax.ipynb cells 8 and 12): orbit g of
+ * n_orb = n_points * per_point belongs to point g / per_point and is integrated
+ * in points[g / per_point] (device array of n_points smx_point; cfg->omega is not
+ * used).  Every other argument is as for smx_integrate, over all n_orb orbits:
+ * w0 SoA (6, n_orb), samples (7, n_orb, slots), info (SMX_INFO_FIELDS, n_orb).
+ * blocks_per_sm caps the resident blocks per SM (0 = as many as fit; a tuning
+ * knob, results do not depend on it).  n_points <= 1024. */
+int smx_integrate_batch(const smx_point *points, int n_points, int64_t per_point, const smx_integrator *cfg,
+                        int precision, const void *w0, const void *dt_init, const void *t_total, int64_t slots,
+                        void *samples, int32_t *n_stored, void *info, int32_t *status, int32_t *queue,
+                        int blocks_per_sm, void *stream);
 
 /* ------------------------------------------------------------- projection */
 typedef struct {
@@ -202,6 +228,16 @@ int smx_project_bin(const smx_binning *geo, int precision, const void *samples,
                     const void *t_total, const int32_t *bin_mapping, const double *num_per_bin,
                     const double *v0, const double *s, void *library, int8_t *valid,
                     void *stream);
+
+/* smx_project_bin for the orbits of n_points parameter points stored one point
+ * after another (as smx_integrate_batch writes them): point q has the rotation
+ * rots[9 q .. 9 q + 8] (device array, row-major like geo->rot, which is not used);
+ * geo->n_part is the particle count of one point.  library (n_points, n_part, rows),
+ * valid (n_points * n_part * n_real). */
+int smx_project_bin_batch(const smx_binning *geo, int n_points, const double *rots, int precision,
+                          const void *samples, const int32_t *n_stored, int64_t slots, const void *info,
+                          const void *t_total, const int32_t *bin_mapping, const double *num_per_bin,
+                          const double *v0, const double *s, void *library, int8_t *valid, void *stream);
 
 /* Cells of individual points (fourfold images when geo->symmetry), with the
  * same arithmetic as smx_project_bin; replaces the index part of bin_chunk

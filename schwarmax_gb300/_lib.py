@@ -28,7 +28,8 @@ SMX_NNLS_FP64, SMX_NNLS_MIXED = 0, 1
 INFO_T, INFO_EJ0, INFO_EJ, INFO_WSUM, INFO_NACC, INFO_NATT, INFO_FIELDS = range(7)
 
 EXPORTS = ["smx_version", "smx_kernel_launches", "smx_status_string", "smx_last_error", "smx_potential_eval",
-           "smx_initial_conditions", "smx_density_target", "smx_integrate", "smx_integrate_noalloc", "smx_project_bin",
+           "smx_initial_conditions", "smx_density_target", "smx_integrate", "smx_integrate_batch", "smx_integrate_noalloc",
+           "smx_project_bin", "smx_project_bin_batch",
            "smx_sample_cells", "smx_soft_project", "smx_soft_project_adjoint", "smx_nnls_workspace_size",
            "smx_nnls_admm", "smx_split_gemm_workspace_size",
            "smx_split_gemm", "smx_model_maps", "smx_model_maps_workspace_size"]
@@ -92,6 +93,10 @@ class SmxPotential(ctypes.Structure):
         "bulge_M", "bulge_a", "bulge_b", "bulge_L", "bulge_gamma")]
 
 
+class SmxPoint(ctypes.Structure):
+    _fields_ = [("pot", SmxPotential), ("omega", ctypes.c_double)]
+
+
 class SmxIntegrator(ctypes.Structure):
     _fields_ = [("mode", ctypes.c_int), ("store_all", ctypes.c_int), ("n_attempts", ctypes.c_int),
                 ("n_samples", ctypes.c_int), ("max_attempts", ctypes.c_int64), ("atol", ctypes.c_double),
@@ -136,6 +141,10 @@ _SIGS = {
                             ctypes.c_double, ctypes.c_double, _P, ctypes.c_int, _P, _P], ctypes.c_int),
     "smx_integrate": ([ctypes.POINTER(SmxPotential), ctypes.POINTER(SmxIntegrator), ctypes.c_int, _P, _P, _P, _I64,
                        _I64, _P, _P, _P, _P, _P, _P], ctypes.c_int),
+    "smx_integrate_batch": ([_P, ctypes.c_int, _I64, ctypes.POINTER(SmxIntegrator), ctypes.c_int, _P, _P, _P, _I64,
+                             _P, _P, _P, _P, _P, ctypes.c_int, _P], ctypes.c_int),
+    "smx_project_bin_batch": ([ctypes.POINTER(SmxBinning), ctypes.c_int, _P, ctypes.c_int, _P, _P, _I64, _P, _P, _P,
+                               _P, _P, _P, _P, _P, _P], ctypes.c_int),
     "smx_integrate_noalloc": ([ctypes.POINTER(SmxPotential), ctypes.POINTER(SmxIntegrator), ctypes.c_int, _P, _P, _P,
                                _I64, _I64, _P, _P, _P, _P, _P], ctypes.c_int),
     "smx_project_bin": ([ctypes.POINTER(SmxBinning), ctypes.c_int, _P, _P, _I64, _P, _P, _P, _P, _P, _P, _P, _P, _P],

@@ -15,6 +15,10 @@
 
 namespace smx {
 
+// The work counter and queue positions are int32: every lane takes one more
+// position than it integrates, so n_orb + (resident threads) must stay below 2^31.
+constexpr int64_t kMaxOrbits = ((int64_t)1 << 31) - ((int64_t)1 << 24);
+
 template <typename T> struct IntegT {
     T atol, rtol, dt_min, dt_max, om;
     int mode, store_all, n_attempts, n_samples;
@@ -54,11 +58,29 @@ __device__ __forceinline__ void put(T *samples, int64_t n_orb, int64_t slots, in
 // that the loop never evaluates forces outside its attempt body.  k1 is parked
 // in slot 0 of the orbit's sample store until the orbit is picked up (its
 // first stored sample overwrites it later); E_J0 goes to its final place.
+// Parameters of one parameter point of a batched call, in the working precision.
+template <typename T> struct PointT {
+    PotT<T> pot;
+    T om;
+};
+
 template <typename T>
-__global__ void __launch_bounds__(128) integrate_init_kernel(PotT<T> P, T om, const T *__restrict__ w0,
+__device__ __forceinline__ PointT<T> make_point(const smx_point &p) {
+    PointT<T> q;
+    q.pot = make_pot<T>(p.pot);
+    q.om = T(p.omega);
+    return q;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) integrate_init_kernel(PotT<T> P0, T om0, const smx_point *__restrict__ points,
+                                                            int64_t per_point, const T *__restrict__ w0,
                                                             int64_t n_orb, int64_t slots, T *samples, T *info) {
     const int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (o >= n_orb) return;
+    const PointT<T> pp = points ? make_point<T>(points[o / per_point]) : PointT<T>{P0, om0};
+    const PotT<T> &P = pp.pot;
+    const T om = pp.om;
     T y[6];
 #pragma unroll
     for (int c = 0; c < 6; ++c) y[c] = w0[c * n_orb + o];
@@ -80,15 +102,28 @@ __global__ void __launch_bounds__(128) integrate_init_kernel(PotT<T> P, T om, co
 // times.  A lane whose orbit ends (attempt cap, all samples emitted, stall or
 // non-finite state) writes its record and loads the next orbit from the queue
 // in the same iteration.
-template <typename T>
-__global__ void __launch_bounds__(128) integrate_kernel(PotT<T> P, IntegT<T> I, const T *__restrict__ w0,
+//
+// BATCH: the orbits of n_points parameter points share one queue (orbit g belongs
+// to point g / per_point); every block copies the points' potentials and frame
+// rates into shared memory, and a lane reads those of its current orbit's point,
+// so that one launch covers the whole batch and the uneven step counts of all its
+// points even out across the SMs.
+template <typename T, bool BATCH>
+__global__ void __launch_bounds__(128) integrate_kernel(PotT<T> P0, IntegT<T> I, const smx_point *__restrict__ points,
+                                                       int n_points, int64_t per_point, const T *__restrict__ w0,
                                                        const T *__restrict__ dt0, const T *__restrict__ t_end,
                                                        int64_t n_orb, int64_t slots, T *samples,
                                                        int32_t *n_stored, T *info, int32_t *status,
                                                        int32_t *queue) {
+    extern __shared__ __align__(16) unsigned char pts_smem[];
+    PointT<T> *spts = reinterpret_cast<PointT<T> *>(pts_smem);
+    if (BATCH) {
+        for (int i = threadIdx.x; i < n_points; i += blockDim.x) spts[i] = make_point<T>(points[i]);
+        __syncthreads();
+    }
     const T e1 = T(-5.0 / 72.0), e2 = T(1.0 / 12.0), e3 = T(1.0 / 9.0), e4 = T(-1.0 / 8.0);
     const T b1 = T(2.0 / 9.0), b2 = T(1.0 / 3.0), b3 = T(4.0 / 9.0);
-    const T om = I.om;
+    int pt = 0;   // parameter point of the current orbit (BATCH)
     const bool sampled = I.mode == SMX_MODE_SAMPLED;
     const int att_cap = sampled ? (int)(I.max_attempts < 0x7fffffffLL ? I.max_attempts : 0x7fffffffLL) : I.n_attempts;
     const int n_samp = I.n_samples;
@@ -112,6 +147,7 @@ __global__ void __launch_bounds__(128) integrate_kernel(PotT<T> P, IntegT<T> I, 
     take();
 
     auto load = [&](int o) {
+        if (BATCH) pt = (int)(o / per_point);
         const T *base = samples + (int64_t)o * slots;
 #pragma unroll
         for (int c = 0; c < 6; ++c) {
@@ -127,6 +163,8 @@ __global__ void __launch_bounds__(128) integrate_kernel(PotT<T> P, IntegT<T> I, 
     if (q < n_orb) load(orb);
 
     while (q < n_orb) {
+        const PotT<T> &P = BATCH ? spts[pt].pot : P0;
+        const T om = BATCH ? spts[pt].om : I.om;
         ++att;
         // stage inputs are formed as soon as their slopes exist, so the stage loop
         // body is one force evaluation plus a uniform branch on s
@@ -249,9 +287,7 @@ __global__ void __launch_bounds__(128) integrate_kernel(PotT<T> P, IntegT<T> I, 
 }
 
 template <typename T>
-static int launch(const smx_potential *pot, const smx_integrator *cfg, const void *w0, const void *dt_init,
-                  const void *t_total, int64_t n_orb, int64_t slots, void *samples, int32_t *n_stored, void *info,
-                  int32_t *status, int32_t *queue, cudaStream_t s) {
+static IntegT<T> make_integ(const smx_integrator *cfg) {
     IntegT<T> I;
     I.atol = T(cfg->atol);
     I.rtol = T(cfg->rtol);
@@ -264,17 +300,34 @@ static int launch(const smx_potential *pot, const smx_integrator *cfg, const voi
     I.n_samples = cfg->n_samples;
     I.max_attempts = cfg->max_attempts;
     I.order = cfg->order;
+    return I;
+}
+
+// points == NULL: one potential (pot, cfg->omega) for all orbits; otherwise the
+// device array of n_points PointT<T> with per_point orbits each.
+template <typename T>
+static int launch(const smx_potential *pot, const smx_integrator *cfg, const smx_point *points, int n_points,
+                  int64_t per_point, const void *w0, const void *dt_init, const void *t_total, int64_t n_orb,
+                  int64_t slots, void *samples, int32_t *n_stored, void *info, int32_t *status, int32_t *queue,
+                  int blocks_per_sm, cudaStream_t s) {
+    const IntegT<T> I = make_integ<T>(cfg);
+    const PotT<T> P0 = points ? PotT<T>() : make_pot<T>(*pot);
+    const int64_t pp = per_point > 0 ? per_point : 1;
     SMX_TRY_CUDA(cudaMemsetAsync(queue, 0, sizeof(int32_t), s));
-    integrate_init_kernel<T><<<(unsigned)((n_orb + 127) / 128), 128, 0, s>>>(make_pot<T>(*pot), T(cfg->omega),
+    integrate_init_kernel<T><<<(unsigned)((n_orb + 127) / 128), 128, 0, s>>>(P0, T(cfg->omega), points, pp,
                                                                          (const T *)w0, n_orb, slots,
                                                                          (T *)samples, (T *)info);
     count_launch();
     int dev = 0, sms = 0;
     SMX_TRY_CUDA(cudaGetDevice(&dev));
     SMX_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const size_t smem = points ? (size_t)n_points * sizeof(PointT<T>) : 0;
+    auto kern = points ? integrate_kernel<T, true> : integrate_kernel<T, false>;
+    if (smem > 48 * 1024) SMX_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
-    SMX_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, integrate_kernel<T>, 128, 0));
+    SMX_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, smem));
     if (per_sm < 1) per_sm = 1;
+    if (blocks_per_sm > 0 && blocks_per_sm < per_sm) per_sm = blocks_per_sm;
     // the same number of blocks on every SM: orbits come from the queue, so every
     // SM keeps working until the queue is empty (512 blocks for 65,536 orbits
     // would put 4 blocks on some SMs and 3 on others)
@@ -282,11 +335,25 @@ static int launch(const smx_potential *pot, const smx_integrator *cfg, const voi
     if (bps > per_sm) bps = per_sm;
     int64_t blocks = (int64_t)sms * bps;
     if (blocks > (n_orb + 127) / 128 * 2 && (n_orb + 127) / 128 < sms) blocks = (n_orb + 127) / 128;   // tiny calls
-    integrate_kernel<T><<<(unsigned)blocks, 128, 0, s>>>(make_pot<T>(*pot), I, (const T *)w0, (const T *)dt_init,
-                                                         (const T *)t_total, n_orb, slots, (T *)samples, n_stored,
-                                                         (T *)info, status, queue);
+    kern<<<(unsigned)blocks, 128, smem, s>>>(P0, I, points, n_points, pp, (const T *)w0, (const T *)dt_init,
+                                             (const T *)t_total, n_orb, slots, (T *)samples, n_stored, (T *)info,
+                                             status, queue);
     count_launch();
     SMX_TRY_CUDA(cudaGetLastError());
+    return SMX_OK;
+}
+
+static int validate_cfg(const smx_integrator *cfg, const void *t_total) {
+    if (cfg->mode == SMX_MODE_REFERENCE) {
+        if (cfg->n_attempts < 1) return set_error(SMX_ERR_ARGUMENT, "n_attempts must be >= 1");
+    } else if (cfg->mode == SMX_MODE_SAMPLED) {
+        if (cfg->n_samples < 1 || cfg->max_attempts < 1 || !t_total)
+            return set_error(SMX_ERR_ARGUMENT, "sampled mode needs n_samples, max_attempts and t_total");
+    } else {
+        return set_error(SMX_ERR_ARGUMENT, "unknown integrator mode %d", cfg->mode);
+    }
+    if (!(cfg->atol > 0) || !(cfg->rtol >= 0) || !(cfg->dt_min > 0) || !(cfg->dt_max >= cfg->dt_min))
+        return set_error(SMX_ERR_ARGUMENT, "bad tolerances or step bounds");
     return SMX_OK;
 }
 
@@ -301,24 +368,45 @@ extern "C" int smx_integrate(const smx_potential *pot, const smx_integrator *cfg
     if (st) return st;
     if (!cfg) return set_error(SMX_ERR_ARGUMENT, "smx_integrate: cfg is NULL");
     if (n_orb < 0 || slots < 1) return set_error(SMX_ERR_ARGUMENT, "smx_integrate: bad sizes");
+    if (n_orb > kMaxOrbits)
+        return set_error(SMX_ERR_UNSUPPORTED, "smx_integrate: n_orb = %lld exceeds the 32-bit work counter's limit of %lld",
+                         (long long)n_orb, (long long)kMaxOrbits);
     if (n_orb == 0) return SMX_OK;
     if (!w0 || !dt_init || !samples || !n_stored || !info || !status || !queue)
         return set_error(SMX_ERR_ARGUMENT, "smx_integrate: NULL buffer");
-    if (cfg->mode == SMX_MODE_REFERENCE) {
-        if (cfg->n_attempts < 1) return set_error(SMX_ERR_ARGUMENT, "n_attempts must be >= 1");
-    } else if (cfg->mode == SMX_MODE_SAMPLED) {
-        if (cfg->n_samples < 1 || cfg->max_attempts < 1 || !t_total)
-            return set_error(SMX_ERR_ARGUMENT, "sampled mode needs n_samples, max_attempts and t_total");
-    } else {
-        return set_error(SMX_ERR_ARGUMENT, "unknown integrator mode %d", cfg->mode);
-    }
-    if (!(cfg->atol > 0) || !(cfg->rtol >= 0) || !(cfg->dt_min > 0) || !(cfg->dt_max >= cfg->dt_min))
-        return set_error(SMX_ERR_ARGUMENT, "bad tolerances or step bounds");
+    if ((st = validate_cfg(cfg, t_total))) return st;
     cudaStream_t s = (cudaStream_t)stream;
     if (precision == SMX_FP32)
-        return launch<float>(pot, cfg, w0, dt_init, t_total, n_orb, slots, samples, n_stored, info, status, queue, s);
+        return launch<float>(pot, cfg, nullptr, 0, 0, w0, dt_init, t_total, n_orb, slots, samples, n_stored, info,
+                             status, queue, 0, s);
     if (precision == SMX_FP64)
-        return launch<double>(pot, cfg, w0, dt_init, t_total, n_orb, slots, samples, n_stored, info, status, queue, s);
+        return launch<double>(pot, cfg, nullptr, 0, 0, w0, dt_init, t_total, n_orb, slots, samples, n_stored, info,
+                              status, queue, 0, s);
+    return set_error(SMX_ERR_ARGUMENT, "bad precision %d", precision);
+}
+
+extern "C" int smx_integrate_batch(const smx_point *points, int n_points, int64_t per_point,
+                                   const smx_integrator *cfg, int precision, const void *w0, const void *dt_init,
+                                   const void *t_total, int64_t slots, void *samples, int32_t *n_stored, void *info,
+                                   int32_t *status, int32_t *queue, int blocks_per_sm, void *stream) {
+    if (!cfg || !points) return set_error(SMX_ERR_ARGUMENT, "smx_integrate_batch: cfg or points is NULL");
+    if (n_points < 1 || n_points > 1024 || per_point < 1 || slots < 1)
+        return set_error(SMX_ERR_ARGUMENT, "smx_integrate_batch: bad sizes (1 <= n_points <= 1024)");
+    const int64_t n_orb = (int64_t)n_points * per_point;
+    if (n_orb > kMaxOrbits)
+        return set_error(SMX_ERR_UNSUPPORTED, "smx_integrate_batch: %lld orbits exceed the 32-bit work counter's limit",
+                         (long long)n_orb);
+    if (!w0 || !dt_init || !samples || !n_stored || !info || !status || !queue)
+        return set_error(SMX_ERR_ARGUMENT, "smx_integrate_batch: NULL buffer");
+    int st;
+    if ((st = validate_cfg(cfg, t_total))) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (precision == SMX_FP32)
+        return launch<float>(nullptr, cfg, points, n_points, per_point, w0, dt_init, t_total, n_orb, slots, samples,
+                             n_stored, info, status, queue, blocks_per_sm, s);
+    if (precision == SMX_FP64)
+        return launch<double>(nullptr, cfg, points, n_points, per_point, w0, dt_init, t_total, n_orb, slots, samples,
+                              n_stored, info, status, queue, blocks_per_sm, s);
     return set_error(SMX_ERR_ARGUMENT, "bad precision %d", precision);
 }
 
@@ -343,7 +431,7 @@ extern "C" int smx_integrate(const smx_potential *pot, const smx_integrator *cfg
 namespace smx {
 
 constexpr int kNoAllocScratchInts = 64;
-constexpr int64_t kNoAllocMaxOrbits = ((int64_t)1 << 31) - ((int64_t)1 << 24);
+constexpr int64_t kNoAllocMaxOrbits = kMaxOrbits;
 constexpr int kNoAllocMaxDevices = 64;
 
 static __device__ __align__(256) int32_t g_noalloc_queue[kNoAllocScratchInts];
@@ -383,24 +471,17 @@ extern "C" int smx_integrate_noalloc(const smx_potential *pot, const smx_integra
     if (n_orb == 0) return SMX_OK;
     if (!w0 || !dt_init || !samples || !n_stored || !info || !status)
         return set_error(SMX_ERR_ARGUMENT, "smx_integrate_noalloc: NULL buffer");
-    if (cfg->mode == SMX_MODE_REFERENCE) {
-        if (cfg->n_attempts < 1) return set_error(SMX_ERR_ARGUMENT, "n_attempts must be >= 1");
-    } else if (cfg->mode == SMX_MODE_SAMPLED) {
-        if (cfg->n_samples < 1 || cfg->max_attempts < 1 || !t_total)
-            return set_error(SMX_ERR_ARGUMENT, "sampled mode needs n_samples, max_attempts and t_total");
-    } else {
-        return set_error(SMX_ERR_ARGUMENT, "unknown integrator mode %d", cfg->mode);
-    }
-    if (!(cfg->atol > 0) || !(cfg->rtol >= 0) || !(cfg->dt_min > 0) || !(cfg->dt_max >= cfg->dt_min))
-        return set_error(SMX_ERR_ARGUMENT, "bad tolerances or step bounds");
+    if ((st = validate_cfg(cfg, t_total))) return st;
     int32_t *queue = nullptr;
     st = noalloc_queue_ptr(&queue);
     if (st) return st;
     cudaStream_t s = (cudaStream_t)stream;
     // launch<T> zeroes the counter on `s` before the kernel
     if (precision == SMX_FP32)
-        return launch<float>(pot, cfg, w0, dt_init, t_total, n_orb, slots, samples, n_stored, info, status, queue, s);
+        return launch<float>(pot, cfg, nullptr, 0, 0, w0, dt_init, t_total, n_orb, slots, samples, n_stored, info,
+                             status, queue, 0, s);
     if (precision == SMX_FP64)
-        return launch<double>(pot, cfg, w0, dt_init, t_total, n_orb, slots, samples, n_stored, info, status, queue, s);
+        return launch<double>(pot, cfg, nullptr, 0, 0, w0, dt_init, t_total, n_orb, slots, samples, n_stored, info,
+                              status, queue, 0, s);
     return set_error(SMX_ERR_ARGUMENT, "bad precision %d", precision);
 }

@@ -2,41 +2,64 @@
 // h_to_V_sigma, ghmoments.py:53-78; the chi^2 / log-likelihood terms of
 // model_likelihood, likelihood.py:192-238).
 //
-// maps = W L^T is one GEMM over all library rows (FP32 SIMT for a float
-// library, FP64 for a double one); a block per weight vector then forms the
-// moments, V, sigma and the chi^2 terms and reduces them in double.  NaN terms
-// are dropped as jnp.nansum does; the Rzphi term is summed over every weight
-// vector and shared, as in the reference.
+// maps = W L^T is one product over all library rows.  For a float library it
+// runs on the bf16 tensor cores as a split (Ozaki) product with FP64-grade
+// accuracy (split_gemm.cuh): the library rows and the weight vectors in 5
+// slices each (39 bits below each row's largest magnitude), so the maps carry
+// no float rounding: the chi^2 summed over 100 bootstraps and several thousand
+// rows moves by O(0.1) when the maps are formed in FP32 arithmetic.  A double
+// library (the plain FP64 path) uses cuBLAS DGEMM.  A block per weight vector
+// then forms the moments, V, sigma and the chi^2 terms and reduces them in
+// double.  NaN terms are dropped as jnp.nansum does; the Rzphi term is summed
+// over every weight vector and shared, as in the reference.
 #include <cublas_v2.h>
 
 #include "smx_internal.cuh"
+#include "split_gemm.cuh"
 
 namespace smx {
 
 struct MapsLayout {
-    size_t Mp, Wf, part, total;
+    size_t Mp, part, total;
+    // split path (float library)
+    split::Operand A, Bw;
+    size_t a_sl, a_e, b_sl, b_e, T, R, rowmax, err;
 };
 
 static inline size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 static MapsLayout maps_layout(const smx_maps_problem *p) {
     MapsLayout L;
-    const size_t rows = (size_t)p->n_cells + 6 * (size_t)p->n_bins;
-    const size_t e = p->lib_precision == SMX_FP32 ? sizeof(float) : sizeof(double);
+    const int64_t rows = (int64_t)p->n_cells + 6 * (int64_t)p->n_bins;
     size_t off = 0;
-    L.Mp = off;
-    off = al256(off + rows * p->n_rhs * e);
-    L.Wf = off;
-    off = al256(off + (p->lib_precision == SMX_FP32 ? (size_t)p->n * p->n_rhs * sizeof(float) : 0));
-    L.part = off;
-    off = al256(off + 2 * p->n_rhs * sizeof(double));
+    auto take = [&](size_t bytes) { size_t o = off; off = al256(off + bytes); return o; };
+    L.Mp = take((size_t)rows * p->n_rhs * sizeof(double));
+    L.part = take(2 * p->n_rhs * sizeof(double));
+    if (p->lib_precision == SMX_FP32) {
+        L.A = split::make_operand(rows, p->n, split::MT, 5);       // library rows over orbits
+        L.Bw = split::make_operand(p->n_rhs, p->n, 112, 5);        // weight vectors over orbits
+        L.a_sl = take(L.A.slice_bytes());
+        L.a_e = take((size_t)L.A.row_tiles * L.A.tile_rows * sizeof(int32_t));
+        L.b_sl = take(L.Bw.slice_bytes());
+        L.b_e = take((size_t)L.Bw.row_tiles * L.Bw.tile_rows * sizeof(int32_t));
+        L.T = take((size_t)rows * p->n_rhs * sizeof(unsigned long long));
+        L.R = take((size_t)rows * p->n_rhs * sizeof(float));
+        L.rowmax = take((size_t)(rows > p->n_rhs ? rows : p->n_rhs) * sizeof(unsigned long long));
+        L.err = take(4 * sizeof(int));
+    }
     L.total = off;
     return L;
 }
 
-__global__ void d2f_kernel(const double *__restrict__ a, float *b, int64_t count) {
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x)
-        b[k] = (float)a[k];
+// Mp = 2^(eA_r + eB_b - 14) (T 2^-t_shift + R), column-major (rows x B)
+__global__ void maps_combine_kernel(const unsigned long long *__restrict__ T, const float *__restrict__ R,
+                                    const int32_t *__restrict__ eA, const int32_t *__restrict__ eB, double *Mp,
+                                    int64_t rows, int64_t B, int t_shift) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < rows * B; k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = k % rows, b = k / rows;
+        const double v = ldexp((double)(long long)T[k], -t_shift) + (double)R[k];
+        Mp[k] = ldexp(v, eA[r] + eB[b] - 14);
+    }
 }
 
 __device__ __forceinline__ double sq_or_zero_nan(double v) {
@@ -105,12 +128,14 @@ __global__ void __launch_bounds__(256) maps_chi2_kernel(const TM *__restrict__ M
     }
 }
 
-__global__ void logl_kernel(const double *__restrict__ part, int64_t B, double *logl) {
+// err (optional): a nonzero code of the split product (a wait that gave up) turns
+// every log-likelihood into NaN, so that a failed product is never taken for a result
+__global__ void logl_kernel(const double *__restrict__ part, int64_t B, const int *err, double *logl) {
     __shared__ double tot;
     if (threadIdx.x == 0) {
         double t = 0;
         for (int64_t b = 0; b < B; ++b) t += part[b];
-        tot = t;
+        tot = (err && err[0]) ? __longlong_as_double(0x7ff8000000000000ll) : t;
     }
     __syncthreads();
     for (int64_t b = threadIdx.x; b < B; b += blockDim.x) logl[b] = -0.5 * (part[B + b] + tot);
@@ -150,37 +175,52 @@ extern "C" int smx_model_maps(const smx_maps_problem *p, const void *library, co
     if (workspace_bytes < L.total)
         return set_error(SMX_ERR_WORKSPACE, "smx_model_maps: workspace %zu < %zu bytes", workspace_bytes, L.total);
     cudaStream_t st = (cudaStream_t)stream;
-    int dev = 0;
-    SMX_TRY_CUDA(cudaGetDevice(&dev));
-    if (g_maps_blas.device != dev) {
-        if (g_maps_blas.h) cublasDestroy(g_maps_blas.h);
-        if (cublasCreate(&g_maps_blas.h) != CUBLAS_STATUS_SUCCESS)
-            return set_error(SMX_ERR_CUDA, "cublasCreate failed");
-        g_maps_blas.device = dev;
-    }
-    cublasHandle_t h = g_maps_blas.h;
-    cublasSetStream(h, st);
-    cublasSetMathMode(h, CUBLAS_DEFAULT_MATH);
     unsigned char *ws = (unsigned char *)workspace;
     const int rows = p->n_cells + 6 * p->n_bins;
     const int64_t n = p->n, B = p->n_rhs;
     double *part = (double *)(ws + L.part);
+    double *Mp = (double *)(ws + L.Mp);
+    const int *errp = nullptr;
     if (p->lib_precision == SMX_FP32) {
-        float *Wf = (float *)(ws + L.Wf);
-        float *Mp = (float *)(ws + L.Mp);
-        const int64_t cnt = n * B;
-        d2f_kernel<<<(unsigned)((cnt + 255) / 256 < 4864 ? (cnt + 255) / 256 : 4864), 256, 0, st>>>(W, Wf, cnt);
+        split::Operand A = L.A, Bw = L.Bw;
+        A.slices = (__nv_bfloat16 *)(ws + L.a_sl);
+        A.expo = (int32_t *)(ws + L.a_e);
+        Bw.slices = (__nv_bfloat16 *)(ws + L.b_sl);
+        Bw.expo = (int32_t *)(ws + L.b_e);
+        unsigned long long *T = (unsigned long long *)(ws + L.T);
+        float *R = (float *)(ws + L.R);
+        int *err = (int *)(ws + L.err);
+        SMX_TRY_CUDA(cudaMemsetAsync(T, 0, (size_t)rows * B * sizeof(unsigned long long), st));
+        SMX_TRY_CUDA(cudaMemsetAsync(R, 0, (size_t)rows * B * sizeof(float), st));
+        SMX_TRY_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
+        unsigned long long *rowmax = (unsigned long long *)(ws + L.rowmax);
+        int sst;
+        // library element (row r, orbit i) at lib[i ld + r];  W element (b, i) at W[b n + i]
+        if ((sst = split::slice_rows<float>((const float *)library, 1, p->ld_lib, A, rowmax, st))) return sst;
+        if ((sst = split::slice_rows<double>(W, n, 1, Bw, rowmax, st))) return sst;
+        split::Acc acc{T, R, rows};
+        if ((sst = split::gemm(A, Bw, acc, false, err, st))) return sst;
+        const int64_t cnt = (int64_t)rows * B;
+        maps_combine_kernel<<<(unsigned)((cnt + 255) / 256 < 4864 ? (cnt + 255) / 256 : 4864), 256, 0, st>>>(
+            T, R, A.expo, Bw.expo, Mp, rows, B, 8 * (split::exact_levels(A, Bw) - 1));
         count_launch();
-        const float one = 1.f, zero = 0.f;
-        cublasStatus_t bs = cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, rows, (int)B, (int)n, &one, (const float *)library,
-                                        (int)p->ld_lib, Wf, (int)n, &zero, Mp, rows);
-        if (bs != CUBLAS_STATUS_SUCCESS) return set_error(SMX_ERR_CUDA, "cublasSgemm (maps) status %d", (int)bs);
-        maps_chi2_kernel<float><<<(unsigned)B, 256, 0, st>>>(Mp, rows, p->n_cells, p->n_bins, gamma_kin, v0, s, y_rz,
-                                                            y_xy, y_xy_boot, y_h_boot, sig_h_raw, B, p->lum_factor,
-                                                            p->sigma_amplify, maps_out, part);
+        maps_chi2_kernel<double><<<(unsigned)B, 256, 0, st>>>(Mp, rows, p->n_cells, p->n_bins, gamma_kin, v0, s, y_rz,
+                                                             y_xy, y_xy_boot, y_h_boot, sig_h_raw, B, p->lum_factor,
+                                                             p->sigma_amplify, maps_out, part);
         count_launch();
+        errp = err;
     } else if (p->lib_precision == SMX_FP64) {
-        double *Mp = (double *)(ws + L.Mp);
+        int dev = 0;
+        SMX_TRY_CUDA(cudaGetDevice(&dev));
+        if (g_maps_blas.device != dev) {
+            if (g_maps_blas.h) cublasDestroy(g_maps_blas.h);
+            if (cublasCreate(&g_maps_blas.h) != CUBLAS_STATUS_SUCCESS)
+                return set_error(SMX_ERR_CUDA, "cublasCreate failed");
+            g_maps_blas.device = dev;
+        }
+        cublasHandle_t h = g_maps_blas.h;
+        cublasSetStream(h, st);
+        cublasSetMathMode(h, CUBLAS_DEFAULT_MATH);
         const double one = 1.0, zero = 0.0;
         cublasStatus_t bs = cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, rows, (int)B, (int)n, &one,
                                         (const double *)library, (int)p->ld_lib, W, (int)n, &zero, Mp, rows);
@@ -192,7 +232,7 @@ extern "C" int smx_model_maps(const smx_maps_problem *p, const void *library, co
     } else {
         return set_error(SMX_ERR_ARGUMENT, "bad library precision %d", p->lib_precision);
     }
-    logl_kernel<<<1, 128, 0, st>>>(part, B, logl_out);
+    logl_kernel<<<1, 128, 0, st>>>(part, B, errp, logl_out);
     count_launch();
     SMX_TRY_CUDA(cudaGetLastError());
     return SMX_OK;

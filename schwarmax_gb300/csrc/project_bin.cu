@@ -10,6 +10,15 @@
 // atomic.  Cell indices follow utils.py:10-42 with explicitly rounded IEEE
 // operations (no FMA contraction), in the order
 //   norm = (p - lo) / (hi - lo); k = floor(norm * n); clip; oob if norm >= 1 or < 0.
+//
+// The row is summed in exact fixed point: every term is rounded once to an
+// integer multiple of 2^-56 and added as an int64, so the sums do not depend on
+// the order of the shared-memory atomics and a library is the same bit for bit
+// from run to run.  With the prescaled weights the Rzphi and xy entries of a
+// column add up to less than 1, and the h_k terms are accumulated before their
+// 1/s_b factor (|g H_k| <= 1 with g = exp(-y^2/2)/sqrt(2 pi)), so every row sum
+// stays below 2^6 and the int64 cannot overflow.  The 1/s_b and the xy
+// normalisation are applied once per entry when the row is written.
 #include "smx_internal.cuh"
 
 namespace smx {
@@ -62,18 +71,18 @@ __device__ __forceinline__ int grid_cell(const T (&v)[D], const T *lo, const T *
 // Rzphi cell (n_cells = outside), Voronoi bin (-1 = outside) and line-of-sight
 // velocity of one phase-space point (integrates.py:120-146).
 template <typename T>
-__device__ __forceinline__ void project_image(const GeoT<T> &G, T x, T y, T z, T vx, T vy, T vz,
+__device__ __forceinline__ void project_image(const GeoT<T> &G, const T *rot, T x, T y, T z, T vx, T vy, T vz,
                                               const int32_t *__restrict__ bin_mapping, int &cell, int &b, T &vl) {
     const T R = RN<T>::sqrt(RN<T>::add(RN<T>::mul(x, x), RN<T>::mul(y, y)));
     const T ph = M<T>::atan2(y, x);
     const T cyl[3] = {R, z, ph};
     cell = grid_cell<T, 3>(cyl, G.lo, G.span, G.fn, G.n, G.n_cells);
-    const T X = RN<T>::add(RN<T>::add(RN<T>::mul(G.rot[0], x), RN<T>::mul(G.rot[1], y)), RN<T>::mul(G.rot[2], z));
-    const T Y = RN<T>::add(RN<T>::add(RN<T>::mul(G.rot[3], x), RN<T>::mul(G.rot[4], y)), RN<T>::mul(G.rot[5], z));
+    const T X = RN<T>::add(RN<T>::add(RN<T>::mul(rot[0], x), RN<T>::mul(rot[1], y)), RN<T>::mul(rot[2], z));
+    const T Y = RN<T>::add(RN<T>::add(RN<T>::mul(rot[3], x), RN<T>::mul(rot[4], y)), RN<T>::mul(rot[5], z));
     const T sky[2] = {X, Y};
     const int pix = grid_cell<T, 2>(sky, G.xlo, G.xspan, G.xfn, G.nx, G.n_pix);
     b = __ldg(&bin_mapping[pix]);
-    vl = RN<T>::add(RN<T>::add(RN<T>::mul(G.rot[6], vx), RN<T>::mul(G.rot[7], vy)), RN<T>::mul(G.rot[8], vz));
+    vl = RN<T>::add(RN<T>::add(RN<T>::mul(rot[6], vx), RN<T>::mul(rot[7], vy)), RN<T>::mul(rot[8], vz));
 }
 
 // Per-sample cells of the fourfold images, for exactness checks and callers
@@ -91,12 +100,20 @@ __global__ void sample_cells_kernel(GeoT<T> G, const T *__restrict__ pts, int64_
         const T sz = (im == 1 || im == 3) ? T(-1) : T(1);
         int cell, b;
         T vl;
-        project_image(G, sxy * q[0], sxy * q[1], sz * q[2], sxy * q[3], sxy * q[4], sz * q[5], bin_mapping, cell, b,
-                      vl);
+        project_image(G, G.rot, sxy * q[0], sxy * q[1], sz * q[2], sxy * q[3], sxy * q[4], sz * q[5], bin_mapping,
+                      cell, b, vl);
         cells[im * N + i] = cell;
         bins[im * N + i] = b;
         if (vlos) vlos[im * N + i] = vl * T(kKpcGyrToKms);
     }
+}
+
+// Adds x rounded to a multiple of 2^-56 (|x| < 2^6) to an int64 fixed-point sum.
+__device__ __forceinline__ void fixed_add(unsigned long long *a, float x) {
+    atomicAdd(a, (unsigned long long)__float2ll_rn(x * 0x1p56f));
+}
+__device__ __forceinline__ void fixed_add(unsigned long long *a, double x) {
+    atomicAdd(a, (unsigned long long)__double2ll_rn(x * 0x1p56));
 }
 
 template <typename T>
@@ -107,14 +124,20 @@ __global__ void __launch_bounds__(256) project_bin_kernel(GeoT<T> G, const T *__
                                                          const double *__restrict__ num_per_bin,
                                                          const double *__restrict__ v0g,
                                                          const double *__restrict__ sg, double area_pixel,
-                                                         T *library, int8_t *valid_out) {
+                                                         const double *__restrict__ rots, T *library,
+                                                         int8_t *valid_out) {
+    // batched calls (rots != NULL): CTA b is particle b % n_part of parameter point
+    // b / n_part, whose rotation is rots[9 point .. 9 point + 8]; the orbits of all
+    // points are numbered consecutively, as smx_integrate_batch stores them
     extern __shared__ unsigned char smem_raw[];
-    T *acc = reinterpret_cast<T *>(smem_raw);
+    unsigned long long *acc = reinterpret_cast<unsigned long long *>(smem_raw);
     __shared__ double scale_r[8];
-    const int p = blockIdx.x;
+    __shared__ T rot[9];
+    const int p = blockIdx.x;   // particle over all points
     const int n_real = G.n_real;
-    const int64_t n_orb = (int64_t)G.n_part * n_real;
-    for (int i = threadIdx.x; i < G.rows; i += blockDim.x) acc[i] = T(0);
+    const int64_t n_orb = (int64_t)G.n_part * n_real * (rots ? (int64_t)gridDim.x / G.n_part : 1);
+    if (threadIdx.x < 9) rot[threadIdx.x] = rots ? T(rots[(p / G.n_part) * 9 + threadIdx.x]) : G.rot[threadIdx.x];
+    for (int i = threadIdx.x; i < G.rows; i += blockDim.x) acc[i] = 0ull;
     if (threadIdx.x == 0) {
         double v[8];
         double nv = 0;
@@ -169,31 +192,33 @@ __global__ void __launch_bounds__(256) project_bin_kernel(GeoT<T> G, const T *__
                 const T vx = sxy * q[3], vy = sxy * q[4], vz = sz * q[5];
                 int cell, b;
                 T vl;
-                project_image(G, x, y, z, vx, vy, vz, bin_mapping, cell, b, vl);
-                if (cell < G.n_cells) atomicAdd(&acc[cell], w);
+                project_image(G, rot, x, y, z, vx, vy, vz, bin_mapping, cell, b, vl);
+                if (cell < G.n_cells) fixed_add(&acc[cell], w);
                 if (b < 0 || b >= nb) continue;
                 const T s_b = T(__ldg(&sg[b]));
                 const T yv = (vl * kms - T(__ldg(&v0g[b]))) / s_b;
-                const T gw = w * isq2pi / s_b * M<T>::exp(T(-0.5) * yv * yv);
+                // g without its 1/s_b (applied when the row is written)
+                const T gw = w * isq2pi * M<T>::exp(T(-0.5) * yv * yv);
                 const T H1 = sq2 * yv;
                 const T H2 = (sq2 * yv * H1 - T(1)) * isq2;
                 const T H3 = (sq2 * yv * H2 - sq2 * H1) * isq3;
                 const T H4 = (sq2 * yv * H3 - sq3 * H2) * T(0.5);
-                atomicAdd(&acc[off_xy + b], w);
-                atomicAdd(&acc[off_h + b], gw);
-                atomicAdd(&acc[off_h + nb + b], gw * H1);
-                atomicAdd(&acc[off_h + 2 * nb + b], gw * H2);
-                atomicAdd(&acc[off_h + 3 * nb + b], gw * H3);
-                atomicAdd(&acc[off_h + 4 * nb + b], gw * H4);
+                fixed_add(&acc[off_xy + b], w);
+                fixed_add(&acc[off_h + b], gw);
+                fixed_add(&acc[off_h + nb + b], gw * H1);
+                fixed_add(&acc[off_h + 2 * nb + b], gw * H2);
+                fixed_add(&acc[off_h + 3 * nb + b], gw * H3);
+                fixed_add(&acc[off_h + 4 * nb + b], gw * H4);
             }
         }
     }
     __syncthreads();
     T *col = library + (int64_t)p * G.rows;
     for (int i = threadIdx.x; i < G.rows; i += blockDim.x) {
-        T v = acc[i];
-        if (i >= off_xy && i < off_h) v = T((double)v / (num_per_bin[i - off_xy] * area_pixel + kEps));
-        col[i] = v;
+        double v = (double)(long long)acc[i] * 0x1p-56;
+        if (i >= off_xy && i < off_h) v = v / (num_per_bin[i - off_xy] * area_pixel + kEps);
+        else if (i >= off_h) v = v / sg[(i - off_h) % nb];
+        col[i] = T(v);
     }
 }
 
@@ -230,9 +255,10 @@ static GeoT<T> make_geo(const smx_binning *g) {
 template <typename T>
 static int launch(const smx_binning *g, const void *samples, const int32_t *n_stored, int64_t slots,
                   const void *info, const void *t_total, const int32_t *bin_mapping, const double *num_per_bin,
-                  const double *v0, const double *s, void *library, int8_t *valid, cudaStream_t st) {
+                  const double *v0, const double *s, void *library, int8_t *valid, cudaStream_t st,
+                  const double *rots = nullptr, int n_points = 1) {
     const GeoT<T> G = make_geo<T>(g);
-    const size_t smem = (size_t)G.rows * sizeof(T);
+    const size_t smem = (size_t)G.rows * sizeof(unsigned long long);
     int dev = 0, max_smem = 0;
     SMX_TRY_CUDA(cudaGetDevice(&dev));
     SMX_TRY_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
@@ -240,9 +266,11 @@ static int launch(const smx_binning *g, const void *samples, const int32_t *n_st
         return set_error(SMX_ERR_UNSUPPORTED, "library row of %d entries does not fit in shared memory", G.rows);
     SMX_TRY_CUDA(cudaFuncSetAttribute(project_bin_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const double area = ((g->X_hi - g->X_lo) / g->nX) * ((g->Y_hi - g->Y_lo) / g->nY) * 1e6;
-    project_bin_kernel<T><<<g->n_part, 256, smem, st>>>(G, (const T *)samples, n_stored, slots, (const T *)info,
-                                                        (const T *)t_total, bin_mapping, num_per_bin, v0, s, area,
-                                                        (T *)library, valid);
+    const int64_t ctas = (int64_t)g->n_part * n_points;
+    if (ctas > 0x7fffffffLL) return set_error(SMX_ERR_UNSUPPORTED, "smx_project_bin: too many particles");
+    project_bin_kernel<T><<<(unsigned)ctas, 256, smem, st>>>(G, (const T *)samples, n_stored, slots, (const T *)info,
+                                                             (const T *)t_total, bin_mapping, num_per_bin, v0, s, area,
+                                                             rots, (T *)library, valid);
     count_launch();
     SMX_TRY_CUDA(cudaGetLastError());
     return SMX_OK;
@@ -273,6 +301,31 @@ extern "C" int smx_project_bin(const smx_binning *geo, int precision, const void
     if (precision == SMX_FP64)
         return launch<double>(geo, samples, n_stored, slots, info, t_total, bin_mapping, num_per_bin, v0, s, library,
                               valid, st);
+    return set_error(SMX_ERR_ARGUMENT, "bad precision %d", precision);
+}
+
+extern "C" int smx_project_bin_batch(const smx_binning *geo, int n_points, const double *rots, int precision,
+                                     const void *samples, const int32_t *n_stored, int64_t slots, const void *info,
+                                     const void *t_total, const int32_t *bin_mapping, const double *num_per_bin,
+                                     const double *v0, const double *s, void *library, int8_t *valid, void *stream) {
+    if (!geo || !rots) return set_error(SMX_ERR_ARGUMENT, "smx_project_bin_batch: geometry or rotations NULL");
+    if (n_points < 1) return set_error(SMX_ERR_ARGUMENT, "smx_project_bin_batch: n_points < 1");
+    if (geo->n_part < 0 || geo->n_real < 1 || geo->n_real > 8 || geo->nR < 1 || geo->nz < 1 || geo->nphi < 1 ||
+        geo->nX < 1 || geo->nY < 1 || geo->n_bins < 1 || slots < 1)
+        return set_error(SMX_ERR_ARGUMENT, "smx_project_bin_batch: bad sizes (n_real must be 1..8)");
+    if (!(geo->R_hi > geo->R_lo) || !(geo->z_hi > geo->z_lo) || !(geo->phi_hi > geo->phi_lo) ||
+        !(geo->X_hi > geo->X_lo) || !(geo->Y_hi > geo->Y_lo))
+        return set_error(SMX_ERR_ARGUMENT, "smx_project_bin_batch: empty grid range");
+    if (geo->n_part == 0) return SMX_OK;
+    if (!samples || !n_stored || !info || !t_total || !bin_mapping || !num_per_bin || !v0 || !s || !library)
+        return set_error(SMX_ERR_ARGUMENT, "smx_project_bin_batch: NULL buffer");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (precision == SMX_FP32)
+        return launch<float>(geo, samples, n_stored, slots, info, t_total, bin_mapping, num_per_bin, v0, s, library,
+                             valid, st, rots, n_points);
+    if (precision == SMX_FP64)
+        return launch<double>(geo, samples, n_stored, slots, info, t_total, bin_mapping, num_per_bin, v0, s, library,
+                              valid, st, rots, n_points);
     return set_error(SMX_ERR_ARGUMENT, "bad precision %d", precision);
 }
 

@@ -89,7 +89,7 @@ template <typename T> struct PotT {
     T ua, ub2, uL, uc1, uc2;                       // V4 bulge
 };
 
-template <typename T> inline PotT<T> make_pot(const smx_potential &p) {
+template <typename T> __host__ __device__ inline PotT<T> make_pot(const smx_potential &p) {
     PotT<T> q;
     q.GMh = T(kG * p.halo_M);
     q.iRs = T(1.0 / p.halo_Rs);

@@ -11,7 +11,10 @@
 //               a tile's k range they add T and R to global memory with atomics.
 // Tensor memory: level 2 at column 0, level 3 at 128, levels >= 4 at 256.
 // Every wait is bounded by a clock deadline; on expiry the CTA records an error
-// code, stops issuing work and leaves after its outstanding operations.
+// code and stops issuing work.  Before it leaves, the copy thread waits for its
+// bulk copies still in flight and the MMA thread commits to a barrier and waits
+// for its MMAs (bounded waits that ignore the abort), and only then is the tensor
+// memory freed.
 #include <cstdio>
 
 #include "smx_internal.cuh"
@@ -60,6 +63,16 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity, volatile
         if (*abort_flag) return false;
         if (clock64() - t0 > (1ll << 31)) return false;
     }
+}
+
+// wait for a phase that is certain to complete (copies or MMAs already issued),
+// ignoring the abort flag, for at most ~2^30 cycles
+__device__ __forceinline__ bool mbar_drain(uint64_t *b, uint32_t parity) {
+    const uint32_t a = smem_u32(b);
+    const long long t0 = clock64();
+    while (!mbar_try(a, parity))
+        if (clock64() - t0 > (1ll << 30)) return false;
+    return true;
 }
 
 __device__ __forceinline__ void mbar_arrive(uint64_t *b) {
@@ -160,7 +173,8 @@ __global__ void __launch_bounds__(320, 1) gemm_kernel(const GemmParams p) {
     uint64_t *empty = full + STAGES;
     uint64_t *acc_full = empty + STAGES;
     uint64_t *acc_empty = acc_full + 1;
-    uint32_t *tmem_holder = (uint32_t *)(acc_empty + 1);
+    uint64_t *mma_done = acc_empty + 1;   // final commit of the MMA thread, waited on before dealloc
+    uint32_t *tmem_holder = (uint32_t *)(mma_done + 1);
     volatile int *abort_flag = (volatile int *)(tmem_holder + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -173,6 +187,7 @@ __global__ void __launch_bounds__(320, 1) gemm_kernel(const GemmParams p) {
         }
         dev::mbar_init(acc_full, 1);
         dev::mbar_init(acc_empty, 8);
+        dev::mbar_init(mma_done, 1);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -213,6 +228,12 @@ __global__ void __launch_bounds__(320, 1) gemm_kernel(const GemmParams p) {
                     dev::bulk_g2s(sbase + SA * C::A_TILE + t * C::B_TILE,
                                   p.B + t * p.b_slice + (nt * p.k_tiles + kt) * (NT * KT), C::B_TILE, full + stage);
             }
+            // no bulk copy may still be landing in shared memory when the CTA leaves:
+            // wait for the last STAGES issued stages (each has exactly one phase
+            // outstanding, since a stage is refilled only after it was consumed).
+            // On the normal path these have completed already.
+            for (int64_t j = (it > STAGES ? it - STAGES : 0); j < it; ++j)
+                if (!dev::mbar_drain(full + (int)(j % STAGES), (uint32_t)((j / STAGES) & 1))) atomicExch(p.err, 5);
         }
     } else if (warp == 1) {
         if (lane == 0) {
@@ -292,6 +313,10 @@ __global__ void __launch_bounds__(320, 1) gemm_kernel(const GemmParams p) {
                     }
                 }
             }
+            // every MMA this thread issued must be complete before the tensor memory
+            // is released, also when the loop above gave up early
+            dev::commit(mma_done);
+            if (!dev::mbar_drain(mma_done, 0)) atomicExch(p.err, 6);
         }
     } else {
         // epilogue: warp w reads lanes 32 (w % 4) .. + 31 (its row quarter), column half h.
@@ -311,9 +336,15 @@ __global__ void __launch_bounds__(320, 1) gemm_kernel(const GemmParams p) {
             const bool tile_end = (u % p.k_tiles == p.k_tiles - 1) || (u + 1 == u1);
             const bool out_flush = tile_end || since_out == OUT_KT;
             if (!(out_flush || since_chunk == C::CHUNK_KT)) continue;
-            if (!dev::mbar_wait(acc_full, flushes & 1, abort_flag)) {
-                if (lane == 0) atomicExch(p.err, 4);
-                *abort_flag = 1;
+            // every lane waits, and the warp goes on only if all of them saw the phase
+            // complete, so that the .sync.aligned tensor-memory loads below run with the
+            // full warp or not at all
+            const bool seen = dev::mbar_wait(acc_full, flushes & 1, abort_flag);
+            if (!__all_sync(0xffffffffu, seen)) {
+                if (lane == 0) {
+                    atomicExch(p.err, 4);
+                    *abort_flag = 1;
+                }
                 break;
             }
             ++flushes;

@@ -309,7 +309,17 @@ def evaluate(pot, params_disk_rho, dd: DeviceData, grid: Grid, st: Settings, nnl
              trajectory=False, want_maps=True):
     """One model evaluation on the device.  Returns a dict of device tensors."""
     libd = build_library(pot, params_disk_rho, dd, grid, st, trajectory=trajectory)
-    lib = libd["library"]
+    r = solve_library(pot, params_disk_rho, dd, grid, st, libd["library"], nnls_maxiter, regularization, weights,
+                      sigma_amplify, want_maps)
+    r["lib"] = libd
+    return r
+
+
+def solve_library(pot, params_disk_rho, dd: DeviceData, grid: Grid, st: Settings, lib, nnls_maxiter=200,
+                  regularization=1.0, weights=(math.sqrt(5.0), math.sqrt(5.0), 1.0), sigma_amplify=1.0,
+                  want_maps=True):
+    """3-D target, data scaling, bootstrap NNLS, maps and chi^2 of one library
+    (model.py:192-272, likelihood.py:192-244)."""
     n = lib.shape[0]
     nc = grid.n_cells
     nb = dd.n_bins
@@ -326,7 +336,79 @@ def evaluate(pot, params_disk_rho, dd: DeviceData, grid: Grid, st: Settings, nnl
     maps, logl = kernels.model_maps(lib, nc, nb, W, d["gamma"].contiguous(), dd.v0, dd.s, d["y_rz"].contiguous(),
                                     dd.xy, y_xy_b, y_h_b, sh_raw, mmpo * d["l2m"], sigma_amplify,
                                     want_maps=want_maps)
-    return dict(lib=libd, data=d, W=W, maps=maps, logl=logl, n_cells=nc, n_bins=nb)
+    return dict(data=d, W=W, maps=maps, logl=logl, n_cells=nc, n_bins=nb)
+
+
+def _batch_bytes_per_point(dd: DeviceData, st: Settings, grid: Grid):
+    el = 4 if st.dtype == torch.float32 else 8
+    pp = dd.n * st.n_real
+    rows = grid.n_cells + 6 * dd.n_bins
+    return pp * (7 * st.slots + 16) * el + dd.n * rows * el
+
+
+def evaluate_batch(pots, barys, dd: DeviceData, grid: Grid, st: Settings, nnls_maxiter=200, regularization=1.0,
+                   weights=(math.sqrt(5.0), math.sqrt(5.0), 1.0), sigma_amplify=1.0, max_points=None,
+                   blocks_per_sm=0, want_maps=False, keep=False):
+    """Model evaluations at P parameter points (jax.vmap(model_likelihood) of the
+    reference's notebooks, example/example_schwarmax.ipynb cells 8 and 12).
+
+    The initial conditions are set up per point; then ONE integrator launch runs
+    the orbits of all points from one work queue (smx_integrate_batch), so the
+    uneven step counts of every point's orbits even out across the SMs, and ONE
+    projection launch bins them with each point's rotation (smx_project_bin_batch).
+    The target, NNLS, maps and chi^2 follow per point.  Points are processed in
+    chunks whose sample store fits the free device memory (max_points caps a chunk).
+    Returns dict(logl (P, B) device tensor, W list, ...)."""
+    P = len(pots)
+    if P != len(barys) or P < 1:
+        raise ValueError("evaluate_batch: one params_disk_rho per potential")
+    if st.mode != "sampled" and st.mode != "reference":
+        raise ValueError(f"unknown mode {st.mode}")
+    dtype = st.dtype
+    n_real = st.n_real
+    pos, normals, uni = dd.cast(dtype, n_real)
+    pp = dd.n * n_real
+    free = torch.cuda.mem_get_info()[0]
+    fit = max(1, int(0.6 * free // _batch_bytes_per_point(dd, st, grid)))
+    chunk = min(P, fit, max_points or P, 1024)
+    mode = SMX_MODE_REFERENCE if st.mode == "reference" else SMX_MODE_SAMPLED
+    cfg = SmxIntegrator(mode=mode, store_all=0, n_attempts=st.n_attempts, n_samples=st.n_samples,
+                        max_attempts=st.max_attempts, atol=st.atol, rtol=st.rtol, dt_min=st.dt_min,
+                        dt_max=st.dt_max, omega=0.0)
+    out = dict(logl=[], W=[], data=[], maps=[], chunk=chunk)
+    for c0 in range(0, P, chunk):
+        c1 = min(P, c0 + chunk)
+        Pc = c1 - c0
+        w0 = torch.empty(6, Pc * pp, dtype=dtype, device="cuda")
+        tt = torch.empty(Pc * pp, dtype=dtype, device="cuda")
+        dt0 = torch.empty(Pc * pp, dtype=dtype, device="cuda")
+        for q in range(Pc):
+            ic = kernels.initial_conditions(pots[c0 + q], pos, normals, uni, n_real, st.n_periods, st.steps_per_period,
+                                            extras=False)
+            sl = slice(q * pp, (q + 1) * pp)
+            w0[:, sl] = ic["w0"]
+            tt[sl] = ic["t_total"]
+            dt0[sl] = ic["dt_init"]
+        pts = kernels.points_tensor(pots[c0:c1], [-float(b["Omega_bar"]) for b in barys[c0:c1]], w0.device)
+        bufs = _integrator_buffers(Pc * pp, st.slots, dtype, role="batch")
+        kernels.integrate_batch(pts, Pc, pp, cfg, w0, dt0, tt, bufs, blocks_per_sm)
+        geo = binning_geometry(barys[c0], grid, dd, n_real)
+        rots = torch.as_tensor(np.stack([rotation_matrix(b["alpha"], b["beta"], b["gamma"]).reshape(-1)
+                                         for b in barys[c0:c1]]), dtype=torch.float64, device="cuda").contiguous()
+        lib = kernels.project_bin_batch(geo, Pc, rots, bufs, tt, dd.bin_mapping, dd.num_per_bin, dd.v0, dd.s)
+        for q in range(Pc):
+            r = solve_library(pots[c0 + q], barys[c0 + q], dd, grid, st, lib[q], nnls_maxiter, regularization, weights,
+                              sigma_amplify, want_maps)
+            out["logl"].append(r["logl"])
+            if keep:
+                out["W"].append(r["W"])
+                out["data"].append(r["data"])
+                out["maps"].append(r["maps"])
+        if keep:
+            out.setdefault("libraries", []).append(lib)
+            out.setdefault("bufs", bufs)
+    out["logl"] = torch.stack(out["logl"])
+    return out
 
 
 def split_maps(maps, nc, nb):

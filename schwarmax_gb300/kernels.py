@@ -10,7 +10,7 @@ import ctypes
 import torch
 
 from . import _lib
-from ._lib import (SmxBinning, SmxIntegrator, SmxMapsProblem, SmxNnlsProblem, SmxPotential, call)
+from ._lib import (SmxBinning, SmxIntegrator, SmxMapsProblem, SmxNnlsProblem, SmxPoint, SmxPotential, call)
 
 DTYPES = {torch.float32: _lib.SMX_FP32, torch.float64: _lib.SMX_FP64}
 
@@ -118,6 +118,62 @@ def integrate(pot, cfg: SmxIntegrator, w0, dt_init, t_total, bufs: IntegratorBuf
          n_orb, bufs.slots, _ptr(bufs.samples), _ptr(bufs.n_stored), _ptr(bufs.info), _ptr(bufs.status),
          _ptr(bufs.queue), _stream())
     return bufs
+
+
+def points_tensor(pots, omegas, device):
+    """Device array of smx_point (potential + frame rate) for a batched call."""
+    arr = (SmxPoint * len(pots))()
+    for i, (p, om) in enumerate(zip(pots, omegas)):
+        arr[i].pot = p
+        arr[i].omega = float(om)
+    raw = bytes(arr)
+    t = torch.frombuffer(bytearray(raw), dtype=torch.uint8).to(device)
+    return t
+
+
+def integrate_batch(points, n_points, per_point, cfg: SmxIntegrator, w0, dt_init, t_total, bufs: IntegratorBuffers,
+                    blocks_per_sm=0):
+    """Orbits of n_points parameter points in one launch (smx_integrate_batch); points is
+    the device array of points_tensor()."""
+    dt = w0.dtype
+    n_orb = w0.shape[1]
+    if n_orb != n_points * per_point:
+        raise ValueError("w0 must hold n_points * per_point orbits")
+    _check(w0, "w0", dt, (6, n_orb))
+    _check(dt_init, "dt_init", dt, (n_orb,))
+    _check(t_total, "t_total", dt, (n_orb,))
+    _check(points, "points", torch.uint8, (n_points * ctypes.sizeof(SmxPoint),))
+    if bufs.n_orb != n_orb or bufs.dtype != dt:
+        raise ValueError("integrator buffers do not match the orbits")
+    call("smx_integrate_batch", _ptr(points), int(n_points), int(per_point), ctypes.byref(cfg), _prec(dt), _ptr(w0),
+         _ptr(dt_init), _ptr(t_total), bufs.slots, _ptr(bufs.samples), _ptr(bufs.n_stored), _ptr(bufs.info),
+         _ptr(bufs.status), _ptr(bufs.queue), int(blocks_per_sm), _stream())
+    return bufs
+
+
+def project_bin_batch(geo: SmxBinning, n_points, rots, bufs: IntegratorBuffers, t_total, bin_mapping, num_per_bin, v0,
+                      s, library=None, valid=None):
+    """smx_project_bin_batch: rots (n_points, 9) double; returns library (n_points, n_part, rows)."""
+    dt = bufs.dtype
+    rows = geo.nR * geo.nz * geo.nphi + 6 * geo.n_bins
+    n_orb = n_points * geo.n_part * geo.n_real
+    if n_orb != bufs.n_orb:
+        raise ValueError("binning geometry does not match the integrated orbits")
+    _check(rots, "rots", torch.float64, (n_points, 9))
+    _check(t_total, "t_total", dt, (n_orb,))
+    _check(bin_mapping, "bin_mapping", torch.int32, (geo.nX * geo.nY + 1,))
+    for t, nm in ((num_per_bin, "num_per_bin"), (v0, "v0"), (s, "s")):
+        _check(t, nm, torch.float64, (geo.n_bins,))
+    dev = bufs.samples.device
+    if library is None:
+        library = torch.empty(n_points, geo.n_part, rows, dtype=dt, device=dev)
+    _check(library, "library", dt, (n_points, geo.n_part, rows))
+    if valid is not None:
+        _check(valid, "valid", torch.int8, (n_orb,))
+    call("smx_project_bin_batch", ctypes.byref(geo), int(n_points), _ptr(rots), _prec(dt), _ptr(bufs.samples),
+         _ptr(bufs.n_stored), bufs.slots, _ptr(bufs.info), _ptr(t_total), _ptr(bin_mapping), _ptr(num_per_bin), _ptr(v0),
+         _ptr(s), _ptr(library), _ptr(valid), _stream())
+    return library
 
 
 def project_bin(geo: SmxBinning, bufs: IntegratorBuffers, t_total, bin_mapping, num_per_bin, v0, s, library=None,

@@ -18,8 +18,8 @@ from .model import model_deltaChi2_jackknife
 from .potentials import density_func, potential_func, potential_struct  # noqa: F401
 from .utils import logMenc_logc_to_logM_logRs
 
-__all__ = ["model_likelihood", "calculate_delta_chi2", "chi2_func", "density_func", "potential_func",
-           "unpack_params"]
+__all__ = ["model_likelihood", "model_likelihood_batch", "calculate_delta_chi2", "chi2_func", "density_func",
+           "potential_func", "unpack_params"]
 
 
 def unpack_params(params):
@@ -64,6 +64,38 @@ def log_likelihoods(params, dict_data, num_Vbin, Rzphi_n_tot, sigma_amplify=1.0,
     pot = potential_struct(bary, halo, st.bulge_mass)
     r = engine.evaluate(pot, bary, dd, grid, st, nnls_maxiter, 1.0, sigma_amplify=sigma_amplify, want_maps=want_maps)
     return r["logl"], r
+
+
+def log_likelihoods_batch(params_batch, dict_data, num_Vbin, Rzphi_n_tot, sigma_amplify=1.0, settings=None,
+                          nnls_maxiter=200, cache=True, max_points=None, blocks_per_sm=0, keep=False):
+    """Bootstrap log-likelihoods (P, N_boot) of P parameter points evaluated as one batch."""
+    st = settings_from(settings)
+    grid = grid_of(dict_data)
+    if grid.n_cells != int(Rzphi_n_tot):
+        raise ValueError("Rzphi_n_tot does not match dict_data['Rzphi_n_grid']")
+    dd = device_data(dict_data, st.n_real, cache=cache)
+    if int(num_Vbin) != dd.n_bins:
+        raise ValueError("num_Vbin does not match dict_data")
+    pots, barys = [], []
+    for th in params_batch:
+        halo, bary = unpack_params(th)
+        pots.append(potential_struct(bary, halo, st.bulge_mass))
+        barys.append(bary)
+    r = engine.evaluate_batch(pots, barys, dd, grid, st, nnls_maxiter, 1.0, sigma_amplify=sigma_amplify,
+                              max_points=max_points, blocks_per_sm=blocks_per_sm, keep=keep)
+    return r["logl"], r
+
+
+def model_likelihood_batch(params_batch, dict_data, num_Vbin, Rzphi_n_tot, sigma_amplify=1.0, settings=None,
+                           nnls_maxiter=200, cache=True, max_points=None):
+    """jax.vmap(model_likelihood) over the rows of params_batch (P, 12), as the
+    reference's grid search and MCMC call it (example/example_schwarmax.ipynb
+    cells 8 and 12).  Returns a NumPy array of the P marginal log-likelihoods."""
+    logl, _ = log_likelihoods_batch(params_batch, dict_data, num_Vbin, Rzphi_n_tot, sigma_amplify, settings,
+                                    nnls_maxiter, cache, max_points)
+    m = torch.max(logl, dim=1, keepdim=True).values
+    lme = m[:, 0] + torch.log(torch.mean(torch.exp(logl - m), dim=1))
+    return lme.cpu().numpy()
 
 
 def log_mean_exp(logl):

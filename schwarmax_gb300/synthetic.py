@@ -53,6 +53,8 @@ class Config:
 CONFIGS = {
     0: Config("config0", 2048, 500, 40, 120, (20, 16, 10), 100),
     1: Config("config1", 16384, 1000, 80, 400, (24, 16, 12), 100),
+    # config 1's library per point, 64 parameter points per batch (points_for)
+    2: Config("config2", 16384, 1000, 80, 400, (24, 16, 12), 100),
     4: Config("config4", 65536, 1000, 120, 1500, (32, 32, 16), 200, bar_mass=2e10, omega_kms_kpc=40.0),
     # config 1 over one circular period with 20 samples: the same orbit count and
     # per-attempt work on a short horizon, for profiler captures
@@ -68,6 +70,20 @@ def theta_for(cfg: Config):
     return np.array([logMenc, math.log10(5e10), math.log10(cfg.bar_mass), logc, math.log10(3.0), math.log10(0.3),
                      math.log10(4.0), math.radians(30.0), math.radians(60.0), math.radians(45.0), 0.0,
                      math.log10(cfg.omega_kms_kpc * KMS_TO_KPCGYR)])
+
+
+def points_for(cfg: Config, n_points, seed=0):
+    """Parameter points of the batched workload: the halo mass and concentration, the
+    disc mass, scale length and height, the bar mass and half-length drawn uniformly
+    within +-20% of the configuration's values, and Omega_p uniform in [25, 45]
+    km/s/kpc; viewing angles and M/L as in theta_for.  Returns (n_points, 12)."""
+    rng = np.random.default_rng(seed)
+    base = theta_for(cfg)
+    out = np.repeat(base[None], n_points, axis=0)
+    for k in (0, 1, 2, 3, 4, 5, 6):          # log10 quantities: +-20% of the value
+        out[:, k] = base[k] + np.log10(rng.uniform(0.8, 1.2, n_points))
+    out[:, 11] = np.log10(rng.uniform(25.0, 45.0, n_points) * KMS_TO_KPCGYR)
+    return out
 
 
 def disc_positions(rng, n, Rd=2.5, zd=0.3):
@@ -99,13 +115,15 @@ def rzphi_grid(n_grid, R_lim=(0.0, 10.0), z_lim=(-3.0, 3.0)):
     return M, [e[1] - e[0] for e in edges]
 
 
-def skeleton(cfg: Config, seed=0, n_part=None):
-    """dict_data without observables: geometry, grids, draws and positions."""
+def skeleton(cfg: Config, seed=0, n_part=None, geometry_seed=None):
+    """dict_data without observables: geometry, grids, draws and positions.  The
+    Voronoi apertures come from geometry_seed (default: seed), the particles and
+    draws from seed, so that a truth library can share the data's apertures."""
     from scipy.stats import qmc
     rng = np.random.default_rng(seed)
     n = cfg.n_part if n_part is None else n_part
     half = cfg.n_pix * cfg.pixel_arcsec * ARCSEC_KPC_AT_50MPC / 2
-    bm, npb = apertures(rng, cfg.n_pix, cfg.n_bins)
+    bm, npb = apertures(rng if geometry_seed is None else np.random.default_rng(geometry_seed), cfg.n_pix, cfg.n_bins)
     M, (dR, dz, dphi) = rzphi_grid(cfg.n_grid)
     d = dict(num_per_bin=npb, bin_mapping=bm, total_bins=cfg.n_bins,
              R_grid=M[:, 0], z_grid=M[:, 1], phi_grid=M[:, 2], R_minmax=[0.0, 10.0], z_minmax=[-3.0, 3.0],
@@ -148,7 +166,8 @@ def _library(cfg, d, theta, v0, s, precision):
 def make_dataset(cfg: Config, seed=0, precision="mixed", noise=True):
     """Returns (dict_data, theta) on the host (NumPy arrays)."""
     theta = theta_for(cfg)
-    truth = skeleton(cfg, seed + 1000)          # independent initial conditions
+    # independent initial conditions and draws on the data's own apertures
+    truth = skeleton(cfg, seed + 1000, geometry_seed=seed)
     nb = cfg.n_bins
     nc = int(np.prod(cfg.n_grid))
     rng = np.random.default_rng(seed + 7)

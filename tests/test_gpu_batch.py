@@ -1,0 +1,116 @@
+"""Batched evaluation over parameter points (jax.vmap(model_likelihood) of the
+reference's notebooks) against per-point evaluations, library determinism, and the
+mixed solver's chi^2 error at the width of the benchmark library."""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def small():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from schwarmax_gb300 import synthetic
+    cfg = synthetic.Config("batch-test", n_part=96, n_samples=60, n_pix=16, n_bins=12, n_grid=(6, 4, 4), n_boot=4,
+                           n_periods=3.0, rtol=1e-5)
+    dd, theta = synthetic.make_dataset(cfg, seed=5, precision="fp64")
+    thetas = np.stack([theta, theta + np.array([0, 0, 0.05, 0, 0, 0, 0, 0.1, -0.1, 0.05, 0.02, 0.03]),
+                       theta + np.array([0, 0.02, -0.05, 0, 0, 0, 0.02, -0.05, 0.05, 0.0, -0.03, -0.04])])
+    return cfg, dd, thetas
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batch_matches_single_points(small, precision):
+    """One integrator launch over all points' orbits (one work queue) and one
+    projection launch with per-point rotations give each point's single-evaluation
+    log-likelihoods."""
+    from schwarmax_gb300.likelihood import log_likelihoods, log_likelihoods_batch
+    cfg, dd, thetas = small
+    st = cfg.settings(precision)
+    nc = int(np.prod(cfg.n_grid))
+    lb, rb = log_likelihoods_batch(thetas, dd, cfg.n_bins, nc, settings=st, nnls_maxiter=80, keep=True)
+    assert lb.shape == (len(thetas), cfg.n_boot)
+    for q, th in enumerate(thetas):
+        ls, rs = log_likelihoods(th, dd, cfg.n_bins, nc, settings=st, nnls_maxiter=80)
+        lib_b = rb["libraries"][0][q]
+        lib_s = rs["lib"]["library"]
+        scale = float(lib_s.abs().max())
+        # the batched kernel reads each point's constants from shared memory, the single
+        # one from kernel parameters; the compiler may contract a multiply-add differently,
+        # and FP32 orbits amplify a rounding difference over the three periods
+        tol = 1e-10 if precision == "fp64" else 2e-3
+        assert float((lib_b - lib_s).abs().max()) <= tol * scale
+        np.testing.assert_allclose(lb[q].cpu().numpy(), ls.cpu().numpy(), rtol=1e-8 if precision == "fp64" else 2e-3)
+
+
+def test_batch_chunks_agree(small):
+    """Splitting the batch into chunks (device memory) changes nothing."""
+    from schwarmax_gb300.likelihood import log_likelihoods_batch
+    cfg, dd, thetas = small
+    st = cfg.settings("fp64")
+    nc = int(np.prod(cfg.n_grid))
+    a, _ = log_likelihoods_batch(thetas, dd, cfg.n_bins, nc, settings=st, nnls_maxiter=40)
+    b, _ = log_likelihoods_batch(thetas, dd, cfg.n_bins, nc, settings=st, nnls_maxiter=40, max_points=2)
+    np.testing.assert_allclose(a.cpu().numpy(), b.cpu().numpy(), rtol=1e-12)
+
+
+def test_model_likelihood_batch_api(small):
+    import schwarmax_gb300 as smx
+    cfg, dd, thetas = small
+    nc = int(np.prod(cfg.n_grid))
+    st = cfg.settings("fp64")
+    v = smx.model_likelihood_batch(thetas, dd, cfg.n_bins, nc, settings=st, nnls_maxiter=40)
+    for q, th in enumerate(thetas):
+        s = smx.model_likelihood(th, dd, cfg.n_bins, nc, settings=st, nnls_maxiter=40)
+        assert abs(v[q] - s) <= 1e-9 * abs(s)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_library_is_deterministic(small, precision):
+    """Exact fixed-point binning: the same samples give the same library bit for bit."""
+    from schwarmax_gb300 import engine
+    from schwarmax_gb300.likelihood import grid_of, unpack_params
+    from schwarmax_gb300.potentials import potential_struct
+    cfg, dd, thetas = small
+    st = cfg.settings(precision)
+    halo, bary = unpack_params(thetas[0])
+    pot = potential_struct(bary, halo, st.bulge_mass)
+    ddv = engine.DeviceData(dd, n_real=st.n_real)
+    a = engine.build_library(pot, bary, ddv, grid_of(dd), st)["library"].clone()
+    b = engine.build_library(pot, bary, ddv, grid_of(dd), st)["library"]
+    assert torch.equal(a, b)
+
+
+def test_mixed_solver_chi2_at_benchmark_width():
+    """Mixed NNLS + maps against FP64 NNLS + maps on one config-1 library
+    (16,384 columns, 4,608 + 5 x 400 = 6,608 design rows, 100 bootstraps, 200
+    iterations): every bootstrap's chi^2 within 0.05 (the metric allows 0.1)."""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from schwarmax_gb300 import engine, kernels, synthetic
+    from schwarmax_gb300.likelihood import log_likelihoods
+    cfg = synthetic.CONFIGS[1]
+    dd, theta = synthetic.make_dataset(cfg, seed=0)
+    st = cfg.settings("mixed")
+    ddv = engine.DeviceData(dd, n_real=st.n_real)
+    nc = int(np.prod(cfg.n_grid))
+    logl_m, r = log_likelihoods(theta, ddv, cfg.n_bins, nc, settings=st, nnls_maxiter=200)
+    lib = r["lib"]["library"]
+    assert lib.shape == (16384, nc + 6 * cfg.n_bins)
+    d = r["data"]
+    row_scale, Y = engine.nnls_inputs(d, ddv, nc, (math.sqrt(5.0), math.sqrt(5.0), 1.0))
+    assert Y.shape == (100, 6608)
+    w_init = float((d["y_rz"].sum() / lib.shape[0]).item())
+    W64 = kernels.nnls_admm(lib.double(), engine.row_map(nc, cfg.n_bins), row_scale, Y, 200, 1.0, w_init,
+                            mixed=False)
+    y_xy_b, y_h_b, sh = engine.likelihood_data(ddv)
+    lum = float(d["mmpo"].item()) * d["l2m"]
+    _, logl_64 = kernels.model_maps(lib.double(), nc, cfg.n_bins, W64, d["gamma"].contiguous(), ddv.v0, ddv.s,
+                                    d["y_rz"].contiguous(), ddv.xy, y_xy_b, y_h_b, sh, lum, 1.0, want_maps=False)
+    dchi2 = (2 * (logl_m - logl_64)).abs()
+    assert float(dchi2.max()) <= 0.05, float(dchi2.max())
+    assert float((r["W"] - W64).abs().max() / W64.abs().max()) <= 1e-6
