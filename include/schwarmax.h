@@ -303,6 +303,24 @@ int smx_nnls_admm(const smx_nnls_problem *prob, const void *library, const int32
                   const double *row_scale, const double *Y, double *Z_out, void *workspace,
                   size_t workspace_bytes, void *stream);
 
+/* Leave-group-out jackknife of the single right-hand-side ADMM NNLS, all
+ * replicates in one batched solve (model_deltaChi2_jackknife, model.py:480-603,
+ * with solve_nnls_admm, nnls.py:6-66, per replicate).  Replicate j solves the
+ * problem of smx_nnls_admm with the design rows drop_rows[j*max_drop ..
+ * (j+1)*max_drop) removed (-1 entries are padding; the reference raises their
+ * sigma to 1e20, which differs from removing them by 1e-40 of ||U||^2): its own
+ * rho_j = tr(Q_j)/n and data row, the shared w_init.  Every replicate's inverse
+ * comes from the one G^-1 of the full problem (Schur complement of the dropped
+ * rows, Neumann series for the shift of rho_j; the number of terms follows the
+ * largest group's share of ||U||_F^2, which must stay below 1/2).  A design row
+ * may be dropped by one replicate at most.  Mixed mode only (split products).
+ *   prob->n_rhs = replicates G;  Y (m) double: the scaled data row;
+ *   drop_rows (G, max_drop) int32, max_drop <= 40;  Z_out (G, n) double. */
+int smx_nnls_jackknife_workspace_size(const smx_nnls_problem *prob, int max_drop, size_t *bytes);
+int smx_nnls_jackknife(const smx_nnls_problem *prob, const void *library, const int32_t *row_map,
+                       const double *row_scale, const double *Y, const int32_t *drop_rows, int max_drop,
+                       double *Z_out, void *workspace, size_t workspace_bytes, void *stream);
+
 /* FP64-accurate product C = A B (A: M x K, B: K x N, C: M x N, all column-major
  * double) on the bf16 tensor cores by Ozaki splitting: every row of A and column
  * of B is scaled by a power of two and split into a_slices / b_slices bf16
@@ -349,6 +367,54 @@ int smx_model_maps(const smx_maps_problem *prob, const void *library, const doub
                    void *workspace, size_t workspace_bytes, void *stream);
 
 int smx_model_maps_workspace_size(const smx_maps_problem *prob, size_t *bytes);
+
+/* ------------------------------------------------------------- post-analysis */
+/* Circular-orbit table of build_Lcirc_of_E (utils.py:275-341): n_grid radii
+ * R_i = np.logspace(log10 R_min, log10 R_max, n_grid) on the x axis,
+ * Vc^2 = max(R (Phi(R + dR) - Phi(R - dR)) / (2 dR), 0), E_i = Phi(R_i) + Vc^2 / 2,
+ * L_i = R_i Vc, all in double.  E_out, L_out (n_grid) double (device). */
+int smx_lcirc_table(const smx_potential *pot, double R_min, double R_max, int n_grid, double dR, double *E_out,
+                    double *L_out, void *stream);
+
+/* Cubic spline (the interp1d(kind='cubic') of build_Lcirc_of_E) at n points x:
+ * knots (n_knots) increasing, coef (4, n_knots - 1) the coefficients of each piece in
+ * powers of (x - knot_j), highest first; below / above: the values outside the knots
+ * (interp1d's fill_value).  x, out (n) double. */
+int smx_spline_eval(const double *knots, const double *coef, int n_knots, double below, double above,
+                    const double *x, int64_t n, double *out, void *stream);
+
+/* Circularity lambda_z = L_z / (L_circ(E) + 1e-10) of n phase-space points (the
+ * analysis of get_model_with_orbit's trajectories, example/example_analysis.ipynb,
+ * model-side circularity cell): E = v^2 / 2 + Phi(x), L_z = -(x v_y - y v_x), v in
+ * kpc/Gyr, L_circ the spline of smx_spline_eval.  points SoA (6, n) of the call's
+ * precision; lam, R (cylindrical radius), E (n) optional outputs. */
+int smx_circularity(const smx_potential *pot, int precision, const void *points, int64_t n, const double *knots,
+                    const double *coef, int n_knots, double L_below, double L_above, void *lam, void *R, void *E,
+                    void *stream);
+
+/* Weighted 2-D histogram with np.histogram2d's binning over the given edges
+ * (edges_a (na + 1), edges_b (nb + 1) increasing double; a value equal to the last
+ * edge falls in the last bin; values outside are dropped).  w may be NULL (weight
+ * 1).  The sums are exact fixed point in units of 2^-40 weight_scale (every |w| and
+ * every bin's sum must stay below 2^23 weight_scale), so the result does not depend
+ * on the order of the adds.  scratch: na * nb uint64; out (na, nb) double. */
+int smx_histogram2d(int precision, const void *a, const void *b, const void *w, int64_t n, const double *edges_a,
+                    int na, const double *edges_b, int nb, double weight_scale, unsigned long long *scratch,
+                    double *out, void *stream);
+
+/* PSF transfer matrix of compute_transfer_matrix (utils.py:413-485): a grid_res^2
+ * fine grid over the field of view (np.linspace edges and centres), each point
+ * assigned to a Voronoi bin through the nX x nY pixel map bin_mapping (nX * nY
+ * entries; -1 = no bin); P[i, j] = sum over fine points q of bin i of the Gaussian
+ * filter of bin j's indicator image at q (separable kernel kernel_weights of
+ * 2 radius + 1 normalised taps, zero outside the grid, as
+ * scipy.ndimage.gaussian_filter(mode='constant')), then every column divided by its
+ * sum.  P (total_bins, total_bins) double, row-major.  Sums are exact fixed point.
+ * At most 16 distinct bins may fall within one row window of the kernel. */
+int smx_psf_transfer_workspace_size(int grid_res, int total_bins, int radius, size_t *bytes);
+int smx_psf_transfer(const double *kernel_weights, int radius, int nX, int nY, double X_lo, double X_hi, double Y_lo,
+                     double Y_hi, const int32_t *bin_mapping, int total_bins, int grid_res, double *P, void *workspace,
+                     size_t workspace_bytes, void *stream);
 
 #ifdef __cplusplus
 }

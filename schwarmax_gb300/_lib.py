@@ -19,7 +19,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(HERE, "libschwarmax_gb300.so")
 SOURCES = ["api.cu", "pointkernels.cu", "integrate.cu", "project_bin.cu", "soft_project.cu", "nnls.cu", "split_gemm.cu",
-           "maps.cu"]
+           "maps.cu", "analysis.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 SMX_FP32, SMX_FP64 = 0, 1
@@ -31,8 +31,9 @@ EXPORTS = ["smx_version", "smx_kernel_launches", "smx_status_string", "smx_last_
            "smx_initial_conditions", "smx_density_target", "smx_integrate", "smx_integrate_batch", "smx_integrate_noalloc",
            "smx_project_bin", "smx_project_bin_batch",
            "smx_sample_cells", "smx_soft_project", "smx_soft_project_adjoint", "smx_nnls_workspace_size",
-           "smx_nnls_admm", "smx_split_gemm_workspace_size",
-           "smx_split_gemm", "smx_model_maps", "smx_model_maps_workspace_size"]
+           "smx_nnls_admm", "smx_nnls_jackknife_workspace_size", "smx_nnls_jackknife", "smx_split_gemm_workspace_size",
+           "smx_split_gemm", "smx_model_maps", "smx_model_maps_workspace_size", "smx_lcirc_table", "smx_spline_eval",
+           "smx_circularity", "smx_histogram2d", "smx_psf_transfer_workspace_size", "smx_psf_transfer"]
 
 
 class SmxError(RuntimeError):
@@ -156,6 +157,22 @@ _SIGS = {
                                   _P, ctypes.c_int64, _P, _P, _P, _P, _P, _P, _P, _P, _P], ctypes.c_int),
     "smx_nnls_workspace_size": ([ctypes.POINTER(SmxNnlsProblem), ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
     "smx_nnls_admm": ([ctypes.POINTER(SmxNnlsProblem), _P, _P, _P, _P, _P, _P, ctypes.c_size_t, _P], ctypes.c_int),
+    "smx_nnls_jackknife_workspace_size": ([ctypes.POINTER(SmxNnlsProblem), ctypes.c_int,
+                                           ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
+    "smx_nnls_jackknife": ([ctypes.POINTER(SmxNnlsProblem), _P, _P, _P, _P, _P, ctypes.c_int, _P, _P, ctypes.c_size_t,
+                            _P], ctypes.c_int),
+    "smx_lcirc_table": ([ctypes.POINTER(SmxPotential), ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                         ctypes.c_double, _P, _P, _P], ctypes.c_int),
+    "smx_spline_eval": ([_P, _P, ctypes.c_int, ctypes.c_double, ctypes.c_double, _P, _I64, _P, _P], ctypes.c_int),
+    "smx_circularity": ([ctypes.POINTER(SmxPotential), ctypes.c_int, _P, _I64, _P, _P, ctypes.c_int, ctypes.c_double,
+                         ctypes.c_double, _P, _P, _P, _P], ctypes.c_int),
+    "smx_histogram2d": ([ctypes.c_int, _P, _P, _P, _I64, _P, ctypes.c_int, _P, ctypes.c_int, ctypes.c_double, _P, _P,
+                         _P], ctypes.c_int),
+    "smx_psf_transfer_workspace_size": ([ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_size_t)],
+                                        ctypes.c_int),
+    "smx_psf_transfer": ([_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                          ctypes.c_double, ctypes.c_double, _P, ctypes.c_int, ctypes.c_int, _P, _P, ctypes.c_size_t,
+                          _P], ctypes.c_int),
     "smx_split_gemm_workspace_size": ([ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int, ctypes.c_int,
                                        ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
     "smx_split_gemm": ([ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P,

@@ -303,6 +303,7 @@ struct ColArgs {
     unsigned long long *colmax;    // max |V| of each column, as ordered bits
     unsigned long long *reset;     // column maxima of another operand, cleared here (n_rhs)
     const double *coefp;
+    const double *colcoef;   // optional per-column k (the jackknife's replicates), else coefp[0]
     double w_init;
     __nv_bfloat16 *slices;   // output operand: n_rhs x K, VS slices, tiles of tile_rows x KT
     int32_t *expo;
@@ -324,7 +325,7 @@ __global__ void __launch_bounds__(256) column_values_kernel(const ColArgs a) {
     if (blockIdx.x == 0 && blockIdx.y == 0)
         for (int i = threadIdx.x; i < a.n_rhs; i += blockDim.x) a.reset[i] = 0ull;
     const int eb = (MODE == COL_INIT) ? 0 : a.eB[j];
-    const double coef = a.coefp[0];
+    const double coef = a.colcoef ? a.colcoef[j] : a.coefp[0];
     const int64_t kb = blockIdx.x * (int64_t)COL_CHUNK;
     const int64_t k1 = kb + COL_CHUNK < K ? kb + COL_CHUNK : K;
     // every load of the thread's PER values is issued before any store, so that
@@ -511,6 +512,132 @@ __global__ void clear_kernel(unsigned long long *T, float *R, int64_t count) {
     }
 }
 
+// The set-up of the mixed path shared by the bootstrap and jackknife solvers: U in
+// double, ||U||_F^2 and the ADMM coefficient, U sliced both ways, G = U U^T + c I
+// from the slices, G^-1 by a float seed and Newton-Schulz steps, and G^-1 split into
+// its diagonal (gdiag) and the sliced off-diagonal part (sh.Xg; Xd keeps it in double).
+struct MixedState {
+    SplitShapes sh;
+    unsigned long long *Tacc, *rowmax;
+    float *Racc;
+    int *derr;
+    double *U, *Xd, *gdiag;
+};
+
+template <typename TL>
+static int mixed_setup(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map, const double *row_scale,
+                       unsigned char *ws, const Layout &L, Handles *h, cudaStream_t s, MixedState &S) {
+    const int64_t m = p->m, n = p->n;
+    const double lam = p->lambda_reg;
+    double *G = (double *)(ws + L.G);
+    double *frob = (double *)(ws + L.frob);
+    int *dinfo = (int *)(ws + L.info);
+    dim3 gb((unsigned)((m + 255) / 256 < 65535 ? (m + 255) / 256 : 65535), (unsigned)(n < 65535 ? n : 65535));
+    // U in double: rounding library x row scale to float (2^-24 of every entry, and
+    // |U|_F^2 and rho with it) moved the bootstrap chi^2 by up to 0.1 at config 1;
+    // the slices below keep 31 bits of each row's largest entry
+    double *U = (double *)(ws + L.U);
+    build_u_kernel<TL, double><<<gb, 256, 0, s>>>(lib, p->ld_lib, row_map, row_scale, m, n, U, dinfo + 3);
+    count_launch();
+    frob_kernel<double><<<grid1d(m * n), 256, 0, s>>>(U, m * n, frob);
+    count_launch();
+    admm_coef_kernel<<<1, 1, 0, s>>>(frob, lam, (double)n, frob + 1);
+    count_launch();
+    SplitShapes sh = split_shapes(p);
+    sh.Ua.slices = (__nv_bfloat16 *)(ws + L.Ua);
+    sh.Ua.expo = (int32_t *)(ws + L.Ua_e);
+    sh.Ut.slices = (__nv_bfloat16 *)(ws + L.Ut);
+    sh.Ut.expo = (int32_t *)(ws + L.Ut_e);
+    sh.Xg.slices = (__nv_bfloat16 *)(ws + L.Xg);
+    sh.Xg.expo = (int32_t *)(ws + L.Xg_e);
+    sh.Ds.slices = (__nv_bfloat16 *)(ws + L.Ds);
+    sh.Ds.expo = (int32_t *)(ws + L.Ds_e);
+    sh.Es.slices = (__nv_bfloat16 *)(ws + L.Es);
+    sh.Es.expo = (int32_t *)(ws + L.Es_e);
+    sh.Fs.slices = (__nv_bfloat16 *)(ws + L.Fs);
+    sh.Fs.expo = (int32_t *)(ws + L.Fs_e);
+    sh.G7.slices = (__nv_bfloat16 *)(ws + L.G7);
+    sh.G7.expo = (int32_t *)(ws + L.G7_e);
+    sh.X7.slices = (__nv_bfloat16 *)(ws + L.X7);
+    sh.X7.expo = (int32_t *)(ws + L.X7_e);
+    sh.X5.slices = (__nv_bfloat16 *)(ws + L.X5);
+    sh.X5.expo = (int32_t *)(ws + L.X5_e);
+    sh.R5.slices = (__nv_bfloat16 *)(ws + L.R5);
+    sh.R5.expo = (int32_t *)(ws + L.R5_e);
+    unsigned long long *Tacc = (unsigned long long *)(ws + L.Tacc);
+    float *Racc = (float *)(ws + L.Racc);
+    unsigned long long *rowmax = (unsigned long long *)(ws + L.rowmax);
+    int *derr = (int *)(ws + L.err);
+    SMX_TRY_CUDA(cudaMemsetAsync(derr, 0, 4 * sizeof(int), s));
+    clear_kernel<<<grid1d(L.acc_elems), 256, 0, s>>>(Tacc, Racc, L.acc_elems);
+    count_launch();
+    // the vector operands' padding (right-hand sides beyond n_rhs) stays zero
+    SMX_TRY_CUDA(cudaMemsetAsync(sh.Ds.slices, 0, sh.Ds.slice_bytes(), s));
+    SMX_TRY_CUDA(cudaMemsetAsync(sh.Es.slices, 0, sh.Es.slice_bytes(), s));
+    SMX_TRY_CUDA(cudaMemsetAsync(sh.Fs.slices, 0, sh.Fs.slice_bytes(), s));
+    int st;
+    // U split both ways: rows of U over orbits (U D, U U^T) and orbits over rows (U^T F)
+    if ((st = split::slice_rows<double>(U, 1, m, sh.Ua, rowmax, s))) return st;
+    if ((st = split::slice_rows<double>(U, m, 1, sh.Ut, rowmax, s))) return st;
+    // G = U U^T + c I from the sliced U (31 bits below each row's largest entry), all slice pairs
+    split::Acc acc{Tacc, Racc, m};
+    float *Gf = (float *)(ws + L.Gf);
+    double *Xd = (double *)(ws + L.Xd), *Rd = (double *)(ws + L.Rd);
+    if ((st = split::gemm(sh.Ua, sh.Ua, acc, true, derr, s))) return st;
+    gram_combine_kernel<<<grid1d(m * m), 256, 0, s>>>(Tacc, Racc, sh.Ua.expo, G, Gf, m, frob, lam, (double)n);
+    count_launch();
+    // G^-1: float Cholesky inverse as the seed, then Newton-Schulz steps
+    //   R = I - G X (diagonals exact, off-diagonal parts as a 7 x 7 split
+    //   product), X <- X + X R.
+    // The new X has residual R^2, whose 2-norm is at most ||R||_F^2: steps
+    // continue until a step's input has ||R||_F <= 3e-7, so the result has
+    // ||I - G X|| <= 1e-13 up to the accuracy of G X times cond(G) (about 2^-44).
+    SMX_TRY_SOLVER(cusolverDnSpotrf(h->solver, CUBLAS_FILL_MODE_LOWER, (int)m, Gf, (int)m, (float *)(ws + L.work),
+                                    L.lwork_s, dinfo));
+    SMX_TRY_SOLVER(cusolverDnSpotri(h->solver, CUBLAS_FILL_MODE_LOWER, (int)m, Gf, (int)m, (float *)(ws + L.work),
+                                    L.lwork_s, dinfo + 1));
+    seed_kernel<<<grid1d(m * m), 256, 0, s>>>(Gf, Xd, m);
+    count_launch();
+    if ((st = split::slice_rows<double>(G, 1, m, sh.G7, rowmax, s, true))) return st;   // O_G
+    double *rss = frob + 3;
+    double fro = 1.0;
+    for (int steps = 0; steps < 6 && fro > 3e-7; ++steps) {
+        if ((st = split::slice_rows<double>(Xd, m, 1, sh.X7, rowmax, s, true))) return st;   // O_X columns over k
+        if ((st = split::gemm(sh.G7, sh.X7, acc, false, derr, s))) return st;
+        SMX_TRY_CUDA(cudaMemsetAsync(rss, 0, sizeof(double), s));
+        ns_residual_kernel<<<grid1d(m * m), 256, 0, s>>>(Tacc, Racc, sh.G7.expo, sh.X7.expo, G, Xd, Rd, m, rss);
+        count_launch();
+        if ((st = split::slice_rows<double>(Xd, 1, m, sh.X5, rowmax, s))) return st;   // X rows over k
+        if ((st = split::slice_rows<double>(Rd, m, 1, sh.R5, rowmax, s))) return st;   // R columns over k
+        if ((st = split::gemm(sh.X5, sh.R5, acc, false, derr, s))) return st;
+        ns_update_kernel<<<grid1d(m * m), 256, 0, s>>>(Tacc, Racc, sh.X5.expo, sh.R5.expo, Xd, m);
+        count_launch();
+        double ss = 0;
+        SMX_TRY_CUDA(cudaMemcpyAsync(&ss, rss, sizeof(ss), cudaMemcpyDeviceToHost, s));
+        SMX_TRY_CUDA(cudaStreamSynchronize(s));
+        fro = sqrt(ss);
+        if (!(fro < 0.5)) break;   // not converging: the seed is too far off
+    }
+    if (!(fro <= 3e-7)) {
+        SMX_TRY_CUDA(cudaStreamSynchronize(s));
+        return set_error(SMX_ERR_NUMERIC, "Newton-Schulz inverse of rho' I + U U^T did not converge (||I - G X||_F %g)",
+                         fro);
+    }
+    double *gdiag = (double *)(ws + L.gdiag);
+    split_diag_kernel<<<grid1d(m), 256, 0, s>>>(Xd, gdiag, m);
+    count_launch();
+    if ((st = split::slice_rows<double>(Xd, 1, m, sh.Xg, rowmax, s))) return st;   // O rows over columns
+    S.sh = sh;
+    S.Tacc = Tacc;
+    S.Racc = Racc;
+    S.rowmax = rowmax;
+    S.derr = derr;
+    S.U = U;
+    S.Xd = Xd;
+    S.gdiag = gdiag;
+    return SMX_OK;
+}
+
 template <typename TL>
 static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map, const double *row_scale,
                const double *Y, double *Z_out, unsigned char *ws, const Layout &L, Handles *h, cudaStream_t s) {
@@ -558,100 +685,14 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
         }
         SMX_TRY_CUDA(cudaMemcpyAsync(Z_out, Z, sizeof(double) * n * B, cudaMemcpyDeviceToDevice, s));
     } else {
-        // U in double: rounding library x row scale to float (2^-24 of every entry, and
-        // |U|_F^2 and rho with it) moved the bootstrap chi^2 by up to 0.1 at config 1;
-        // the slices below keep 31 bits of each row's largest entry
-        double *U = (double *)(ws + L.U);
-        build_u_kernel<TL, double><<<gb, 256, 0, s>>>(lib, p->ld_lib, row_map, row_scale, m, n, U, dinfo + 3);
-        count_launch();
-        frob_kernel<double><<<grid1d(m * n), 256, 0, s>>>(U, m * n, frob);
-        count_launch();
-        admm_coef_kernel<<<1, 1, 0, s>>>(frob, lam, (double)n, frob + 1);
-        count_launch();
-        SplitShapes sh = split_shapes(p);
-        sh.Ua.slices = (__nv_bfloat16 *)(ws + L.Ua);
-        sh.Ua.expo = (int32_t *)(ws + L.Ua_e);
-        sh.Ut.slices = (__nv_bfloat16 *)(ws + L.Ut);
-        sh.Ut.expo = (int32_t *)(ws + L.Ut_e);
-        sh.Xg.slices = (__nv_bfloat16 *)(ws + L.Xg);
-        sh.Xg.expo = (int32_t *)(ws + L.Xg_e);
-        sh.Ds.slices = (__nv_bfloat16 *)(ws + L.Ds);
-        sh.Ds.expo = (int32_t *)(ws + L.Ds_e);
-        sh.Es.slices = (__nv_bfloat16 *)(ws + L.Es);
-        sh.Es.expo = (int32_t *)(ws + L.Es_e);
-        sh.Fs.slices = (__nv_bfloat16 *)(ws + L.Fs);
-        sh.Fs.expo = (int32_t *)(ws + L.Fs_e);
-        sh.G7.slices = (__nv_bfloat16 *)(ws + L.G7);
-        sh.G7.expo = (int32_t *)(ws + L.G7_e);
-        sh.X7.slices = (__nv_bfloat16 *)(ws + L.X7);
-        sh.X7.expo = (int32_t *)(ws + L.X7_e);
-        sh.X5.slices = (__nv_bfloat16 *)(ws + L.X5);
-        sh.X5.expo = (int32_t *)(ws + L.X5_e);
-        sh.R5.slices = (__nv_bfloat16 *)(ws + L.R5);
-        sh.R5.expo = (int32_t *)(ws + L.R5_e);
-        unsigned long long *Tacc = (unsigned long long *)(ws + L.Tacc);
-        float *Racc = (float *)(ws + L.Racc);
-        unsigned long long *rowmax = (unsigned long long *)(ws + L.rowmax);
-        int *derr = (int *)(ws + L.err);
-        SMX_TRY_CUDA(cudaMemsetAsync(derr, 0, 4 * sizeof(int), s));
-        clear_kernel<<<grid1d(L.acc_elems), 256, 0, s>>>(Tacc, Racc, L.acc_elems);
-        count_launch();
-        // the vector operands' padding (right-hand sides beyond n_rhs) stays zero
-        SMX_TRY_CUDA(cudaMemsetAsync(sh.Ds.slices, 0, sh.Ds.slice_bytes(), s));
-        SMX_TRY_CUDA(cudaMemsetAsync(sh.Es.slices, 0, sh.Es.slice_bytes(), s));
-        SMX_TRY_CUDA(cudaMemsetAsync(sh.Fs.slices, 0, sh.Fs.slice_bytes(), s));
+        MixedState S;
         int st;
-        // U split both ways: rows of U over orbits (U D, U U^T) and orbits over rows (U^T F)
-        if ((st = split::slice_rows<double>(U, 1, m, sh.Ua, rowmax, s))) return st;
-        if ((st = split::slice_rows<double>(U, m, 1, sh.Ut, rowmax, s))) return st;
-        // G = U U^T + c I from the sliced U (31 bits below each row's largest entry), all slice pairs
-        split::Acc acc{Tacc, Racc, m};
-        float *Gf = (float *)(ws + L.Gf);
-        double *Xd = (double *)(ws + L.Xd), *Rd = (double *)(ws + L.Rd);
-        if ((st = split::gemm(sh.Ua, sh.Ua, acc, true, derr, s))) return st;
-        gram_combine_kernel<<<grid1d(m * m), 256, 0, s>>>(Tacc, Racc, sh.Ua.expo, G, Gf, m, frob, lam, (double)n);
-        count_launch();
-        // G^-1: float Cholesky inverse as the seed, then Newton-Schulz steps
-        //   R = I - G X (diagonals exact, off-diagonal parts as a 7 x 7 split
-        //   product), X <- X + X R.
-        // The new X has residual R^2, whose 2-norm is at most ||R||_F^2: steps
-        // continue until a step's input has ||R||_F <= 3e-7, so the result has
-        // ||I - G X|| <= 1e-13 up to the accuracy of G X times cond(G) (about 2^-44).
-        SMX_TRY_SOLVER(cusolverDnSpotrf(h->solver, CUBLAS_FILL_MODE_LOWER, (int)m, Gf, (int)m, (float *)(ws + L.work),
-                                        L.lwork_s, dinfo));
-        SMX_TRY_SOLVER(cusolverDnSpotri(h->solver, CUBLAS_FILL_MODE_LOWER, (int)m, Gf, (int)m, (float *)(ws + L.work),
-                                        L.lwork_s, dinfo + 1));
-        seed_kernel<<<grid1d(m * m), 256, 0, s>>>(Gf, Xd, m);
-        count_launch();
-        if ((st = split::slice_rows<double>(G, 1, m, sh.G7, rowmax, s, true))) return st;   // O_G
-        double *rss = frob + 3;
-        double fro = 1.0;
-        for (int steps = 0; steps < 6 && fro > 3e-7; ++steps) {
-            if ((st = split::slice_rows<double>(Xd, m, 1, sh.X7, rowmax, s, true))) return st;   // O_X columns over k
-            if ((st = split::gemm(sh.G7, sh.X7, acc, false, derr, s))) return st;
-            SMX_TRY_CUDA(cudaMemsetAsync(rss, 0, sizeof(double), s));
-            ns_residual_kernel<<<grid1d(m * m), 256, 0, s>>>(Tacc, Racc, sh.G7.expo, sh.X7.expo, G, Xd, Rd, m, rss);
-            count_launch();
-            if ((st = split::slice_rows<double>(Xd, 1, m, sh.X5, rowmax, s))) return st;   // X rows over k
-            if ((st = split::slice_rows<double>(Rd, m, 1, sh.R5, rowmax, s))) return st;   // R columns over k
-            if ((st = split::gemm(sh.X5, sh.R5, acc, false, derr, s))) return st;
-            ns_update_kernel<<<grid1d(m * m), 256, 0, s>>>(Tacc, Racc, sh.X5.expo, sh.R5.expo, Xd, m);
-            count_launch();
-            double ss = 0;
-            SMX_TRY_CUDA(cudaMemcpyAsync(&ss, rss, sizeof(ss), cudaMemcpyDeviceToHost, s));
-            SMX_TRY_CUDA(cudaStreamSynchronize(s));
-            fro = sqrt(ss);
-            if (!(fro < 0.5)) break;   // not converging: the seed is too far off
-        }
-        if (!(fro <= 3e-7)) {
-            SMX_TRY_CUDA(cudaStreamSynchronize(s));
-            return set_error(SMX_ERR_NUMERIC, "Newton-Schulz inverse of rho' I + U U^T did not converge (||I - G X||_F %g)",
-                             fro);
-        }
-        double *gdiag = (double *)(ws + L.gdiag), *Ebuf = (double *)(ws + L.Ebuf);
-        split_diag_kernel<<<grid1d(m), 256, 0, s>>>(Xd, gdiag, m);
-        count_launch();
-        if ((st = split::slice_rows<double>(Xd, 1, m, sh.Xg, rowmax, s))) return st;   // O rows over columns
+        if ((st = mixed_setup<TL>(p, lib, row_map, row_scale, ws, L, h, s, S))) return st;
+        SplitShapes &sh = S.sh;
+        unsigned long long *Tacc = S.Tacc;
+        float *Racc = S.Racc;
+        int *derr = S.derr;
+        double *gdiag = S.gdiag, *Ebuf = (double *)(ws + L.Ebuf);
         double *Z = (double *)(ws + L.Z), *Uu = (double *)(ws + L.Uu), *D = (double *)(ws + L.D);
         const double *coefp = frob + 1;
         // column maxima of the three vector operands (D, E, F), cleared once here and
@@ -675,6 +716,7 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
             a.Uu = Uu;
             a.D = D;
             a.coefp = coefp;
+            a.colcoef = nullptr;
             a.w_init = p->w_init;
             a.slices = out.slices;
             a.expo = out.expo;
@@ -734,6 +776,384 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
     return SMX_OK;
 }
 
+// ------------------------------------------------------------------ jackknife
+// Leave-group-out replicates of the single right-hand-side solve
+// (model_deltaChi2_jackknife, model.py:480-603): replicate j raises sigma of the
+// rows of its group to 1e20, i.e. drops rows d_j of U and y.  All replicates run
+// as the columns of one batched ADMM and share one G^-1 of the full problem:
+//   * rho_j = rho - delta_j with delta_j = ||U_dj||_F^2 / n, c_j = c - delta_j;
+//   * on the kept rows K the replicate's Woodbury matrix is G_KK - delta_j I, whose
+//     inverse is sum_i delta_j^i S^(i+1) (Neumann series, ||delta_j S|| <= delta_j / c)
+//     with S = (G_KK)^-1 = [X - X_{:,d} (X_dd)^-1 X_{d,:}]_KK, X = G^-1 (Schur
+//     complement of the dropped rows);
+//   * every term is one product with the off-diagonal part O of X for all replicates
+//     (split product) plus a rank-|d_j| correction per replicate.
+// Dropped rows of the residual and of every term are zero, so U^T F never sees them.
+// The reference's 1e-20-scaled rows differ from removed rows by 1e-40 of ||U||^2.
+
+// row_group[r] = the replicate that drops design row r (-1: none); flag 1: a row out
+// of range, 2: a row in two groups
+__global__ void jk_rowgroup_kernel(const int32_t *__restrict__ drop, int max_drop, int64_t G, int64_t m,
+                                   int32_t *row_group, int *flag) {
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < G * max_drop;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t r = drop[idx];
+        if (r < 0) continue;
+        if (r >= m) {
+            atomicExch(flag, 1);
+            continue;
+        }
+        const int32_t j = (int32_t)(idx / max_drop);
+        const int32_t old = atomicCAS(row_group + r, -1, j);
+        if (old != -1 && old != j) atomicExch(flag, 2);
+    }
+}
+
+// ||U_r||^2 of every design row (U column-major m x n); grid (rows / 256, k splits)
+__global__ void rownorm_kernel(const double *__restrict__ U, int64_t m, int64_t n, double *out) {
+    const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (r >= m) return;
+    const int64_t kc = (n + gridDim.y - 1) / gridDim.y;
+    const int64_t k0 = blockIdx.y * kc, k1 = k0 + kc < n ? k0 + kc : n;
+    double acc = 0;
+    for (int64_t i = k0; i < k1; ++i) {
+        const double v = U[i * m + r];
+        acc += v * v;
+    }
+    atomicAdd(out + r, acc);
+}
+
+constexpr int JK_MAX_DROP = 40;
+
+// One thread per replicate: its coefficient k_j, Neumann factor delta_j, and Z_j =
+// (X_dd)^-1 (Gauss-Jordan without pivoting: X_dd is symmetric positive definite).
+// qmax receives max_j delta_j / c as ordered bits.
+__global__ void jk_setup_kernel(const int32_t *__restrict__ drop, int max_drop, int64_t G,
+                                const double *__restrict__ rownorm, const double *__restrict__ frob, double lambda,
+                                double n, const double *__restrict__ O, const double *__restrict__ g, int64_t m,
+                                double *kcoef, double *mu, double *Zinv, unsigned long long *qmax, int *flag) {
+    const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (j >= G) return;
+    const int32_t *d = drop + j * max_drop;
+    int sz = 0;
+    double delta = 0;
+    for (int a = 0; a < max_drop; ++a)
+        if (d[a] >= 0) {
+            delta += rownorm[d[a]];
+            ++sz;
+        }
+    delta /= n;
+    const double rho = (frob[0] + lambda) / n, c = rho + lambda / n;
+    const double rho_j = rho - delta, c_j = c - delta;
+    kcoef[j] = rho_j / c_j;
+    mu[j] = delta;
+    atomicMax(qmax, (unsigned long long)__double_as_longlong(delta / c));
+    double *A = Zinv + j * (int64_t)max_drop * max_drop;
+    // compact the dropped rows to the first sz entries of A's index space
+    int idx[JK_MAX_DROP];
+    int q = 0;
+    for (int a = 0; a < max_drop; ++a)
+        if (d[a] >= 0) idx[q++] = d[a];
+    for (int a = 0; a < sz; ++a)
+        for (int b = 0; b < sz; ++b)
+            A[a * max_drop + b] = (a == b) ? g[idx[a]] : O[idx[a] + m * (int64_t)idx[b]];
+    for (int k = 0; k < sz; ++k) {
+        const double piv = A[k * max_drop + k];
+        if (!(piv > 0)) {
+            atomicExch(flag, 3);
+            return;
+        }
+        const double ip = 1.0 / piv;
+        for (int b = 0; b < sz; ++b) A[k * max_drop + b] *= ip;
+        A[k * max_drop + k] = ip;
+        for (int a = 0; a < sz; ++a) {
+            if (a == k) continue;
+            const double f = A[a * max_drop + k];
+            if (f == 0.0) continue;
+            for (int b = 0; b < sz; ++b) A[a * max_drop + b] -= f * A[k * max_drop + b];
+            A[a * max_drop + k] = -f * ip;
+        }
+    }
+}
+
+// E = Y - U D with the replicate's dropped rows set to 0; Y is the shared data row.
+// Grid (K / COL_CHUNK, replicates).  T, R of the product are cleared.
+__global__ void __launch_bounds__(256) jk_resid_kernel(const ColArgs a, const int32_t *__restrict__ row_group) {
+    constexpr int PER = COL_CHUNK / 256;
+    const int64_t j = blockIdx.y, K = a.K;
+    const int eb = a.eB[j];
+    const int64_t kb = blockIdx.x * (int64_t)COL_CHUNK;
+    double mx = 0;
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+        const int64_t k = kb + threadIdx.x + q * 256, idx = k + K * j;
+        if (k >= K) continue;
+        const double pv = product_of((long long)a.T[idx], a.R[idx], a.eA[k], eb, a.t_shift);
+        a.T[idx] = 0ull;
+        a.R[idx] = 0.0f;
+        const double v = row_group[k] == (int32_t)j ? 0.0 : a.Y[k] - pv;
+        a.E[idx] = v;
+        mx = fmax(mx, fabs(v));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    __shared__ double red[8];
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m2 = 0;
+        for (int w = 0; w < 8; ++w) m2 = fmax(m2, red[w]);
+        atomicMax(a.colmax + j, (unsigned long long)__double_as_longlong(m2));
+    }
+}
+
+// One thread per replicate: c_j = Z_j (O V)_{d_j}  (V vanishes on d_j, so the term's
+// value on the dropped rows is the product alone)
+__global__ void jk_dvals_kernel(const unsigned long long *__restrict__ T, const float *__restrict__ R,
+                                const int32_t *__restrict__ eA, const int32_t *__restrict__ eB, int t_shift,
+                                const int32_t *__restrict__ drop, int max_drop, int64_t G, int64_t m,
+                                const double *__restrict__ Zinv, double *cbuf) {
+    const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (j >= G) return;
+    const int32_t *d = drop + j * max_drop;
+    double pd[JK_MAX_DROP];
+    int sz = 0;
+    for (int a = 0; a < max_drop; ++a)
+        if (d[a] >= 0) {
+            const int64_t idx = d[a] + m * j;
+            pd[sz++] = product_of((long long)T[idx], R[idx], eA[d[a]], eB[j], t_shift);
+        }
+    const double *Z = Zinv + j * (int64_t)max_drop * max_drop;
+    for (int a = 0; a < sz; ++a) {
+        double c = 0;
+        for (int b = 0; b < sz; ++b) c += Z[a * max_drop + b] * pd[b];
+        cbuf[j * max_drop + a] = c;
+    }
+}
+
+// One Neumann term for every replicate, grid (K / COL_CHUNK, replicates):
+//   P = g V + O V - X_{:,d} c  (P = 0 on d),  F (+)= P,  V = delta_j P,
+// and the column maxima of the operand sliced next (V, or F after the last term).
+__global__ void __launch_bounds__(256) jk_apply_kernel(const ColArgs a, const int32_t *__restrict__ row_group,
+                                                       const int32_t *__restrict__ drop, int max_drop,
+                                                       const double *__restrict__ O, const double *__restrict__ cbuf,
+                                                       const double *__restrict__ mu, double *F, int first, int last) {
+    constexpr int PER = COL_CHUNK / 256;
+    const int64_t j = blockIdx.y, K = a.K;
+    const int eb = a.eB[j];
+    __shared__ int32_t dr[JK_MAX_DROP];
+    __shared__ double cc[JK_MAX_DROP];
+    __shared__ int sz;
+    if (threadIdx.x == 0) {
+        int q = 0;
+        for (int t = 0; t < max_drop; ++t) {
+            const int32_t r = drop[j * max_drop + t];
+            if (r >= 0) {
+                dr[q] = r;
+                cc[q] = cbuf[j * max_drop + q];
+                ++q;
+            }
+        }
+        sz = q;
+    }
+    __syncthreads();
+    const double muj = mu[j];
+    const int64_t kb = blockIdx.x * (int64_t)COL_CHUNK;
+    double mx = 0;
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+        const int64_t k = kb + threadIdx.x + q * 256, idx = k + K * j;
+        if (k >= K) continue;
+        const double pv = product_of((long long)a.T[idx], a.R[idx], a.eA[k], eb, a.t_shift);
+        a.T[idx] = 0ull;
+        a.R[idx] = 0.0f;
+        double P = 0.0;
+        if (row_group[k] != (int32_t)j) {
+            P = a.g[k] * a.E[idx] + pv;
+            for (int t = 0; t < sz; ++t) P -= O[k + K * (int64_t)dr[t]] * cc[t];
+        }
+        const double f = first ? P : F[idx] + P;
+        F[idx] = f;
+        const double v = muj * P;
+        a.E[idx] = v;
+        mx = fmax(mx, fabs(last ? f : v));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    __shared__ double red[8];
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m2 = 0;
+        for (int w = 0; w < 8; ++w) m2 = fmax(m2, red[w]);
+        atomicMax(a.colmax + j, (unsigned long long)__double_as_longlong(m2));
+    }
+}
+
+struct JkLayout {
+    size_t rownorm, kcoef, mu, Zinv, cbuf, rowgrp, qmax, flag, dummy, total;
+};
+
+static JkLayout jk_layout(size_t base, int64_t m, int64_t G, int max_drop) {
+    JkLayout J;
+    size_t off = base;
+    auto take = [&](size_t bytes) { size_t o = off; off = align256(off + bytes); return o; };
+    J.rownorm = take(m * sizeof(double));
+    J.kcoef = take(G * sizeof(double));
+    J.mu = take(G * sizeof(double));
+    J.Zinv = take((size_t)G * max_drop * max_drop * sizeof(double));
+    J.cbuf = take((size_t)G * max_drop * sizeof(double));
+    J.rowgrp = take(m * sizeof(int32_t));
+    J.qmax = take(sizeof(unsigned long long));
+    J.flag = take(4 * sizeof(int));
+    J.dummy = take(G * sizeof(unsigned long long));
+    J.total = off;
+    return J;
+}
+
+template <typename TL>
+static int run_jackknife(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map, const double *row_scale,
+                         const double *Y, const int32_t *drop, int max_drop, double *Z_out, unsigned char *ws,
+                         const Layout &L, const JkLayout &J, Handles *h, cudaStream_t s) {
+    const int64_t m = p->m, n = p->n, B = p->n_rhs;
+    double *frob = (double *)(ws + L.frob);
+    int *dinfo = (int *)(ws + L.info);
+    int *jflag = (int *)(ws + J.flag);
+    SMX_TRY_CUDA(cudaMemsetAsync(frob, 0, sizeof(double), s));
+    SMX_TRY_CUDA(cudaMemsetAsync(dinfo, 0, 4 * sizeof(int), s));
+    SMX_TRY_CUDA(cudaMemsetAsync(jflag, 0, 4 * sizeof(int), s));
+    MixedState S;
+    int st;
+    if ((st = mixed_setup<TL>(p, lib, row_map, row_scale, ws, L, h, s, S))) return st;
+    SplitShapes &sh = S.sh;
+    double *rownorm = (double *)(ws + J.rownorm), *kcoef = (double *)(ws + J.kcoef), *mu = (double *)(ws + J.mu);
+    double *Zinv = (double *)(ws + J.Zinv), *cbuf = (double *)(ws + J.cbuf);
+    int32_t *rowgrp = (int32_t *)(ws + J.rowgrp);
+    unsigned long long *qmax = (unsigned long long *)(ws + J.qmax);
+    SMX_TRY_CUDA(cudaMemsetAsync(rownorm, 0, m * sizeof(double), s));
+    SMX_TRY_CUDA(cudaMemsetAsync(rowgrp, 0xff, m * sizeof(int32_t), s));
+    SMX_TRY_CUDA(cudaMemsetAsync(qmax, 0, sizeof(unsigned long long), s));
+    jk_rowgroup_kernel<<<grid1d(B * max_drop), 256, 0, s>>>(drop, max_drop, B, m, rowgrp, jflag);
+    count_launch();
+    rownorm_kernel<<<dim3((unsigned)((m + 255) / 256), 64), 256, 0, s>>>(S.U, m, n, rownorm);
+    count_launch();
+    jk_setup_kernel<<<(unsigned)((B + 63) / 64), 64, 0, s>>>(drop, max_drop, B, rownorm, frob, p->lambda_reg,
+                                                             (double)n, S.Xd, S.gdiag, m, kcoef, mu, Zinv, qmax,
+                                                             jflag + 1);
+    count_launch();
+    // the number of Neumann terms follows the largest delta_j / c (one read-back)
+    unsigned long long hq = 0;
+    int hflag[4] = {0, 0, 0, 0};
+    SMX_TRY_CUDA(cudaMemcpyAsync(&hq, qmax, sizeof(hq), cudaMemcpyDeviceToHost, s));
+    SMX_TRY_CUDA(cudaMemcpyAsync(hflag, jflag, sizeof(hflag), cudaMemcpyDeviceToHost, s));
+    SMX_TRY_CUDA(cudaStreamSynchronize(s));
+    if (hflag[0] == 1) return set_error(SMX_ERR_ARGUMENT, "smx_nnls_jackknife: a dropped row is outside [0, m)");
+    if (hflag[0] == 2) return set_error(SMX_ERR_ARGUMENT, "smx_nnls_jackknife: a design row is dropped by two replicates");
+    if (hflag[1]) return set_error(SMX_ERR_NUMERIC, "smx_nnls_jackknife: the dropped rows' block of G^-1 is not positive");
+    double qv;
+    memcpy(&qv, &hq, sizeof(qv));
+    if (!(qv < 0.5))
+        return set_error(SMX_ERR_UNSUPPORTED, "smx_nnls_jackknife: a group carries %.3g of ||U||_F^2 (at most 0.5)", qv);
+    int terms = 1;
+    for (double t = qv; t > 1e-15 && terms < 64; t *= qv) ++terms;
+    double *Z = (double *)(ws + L.Z), *Uu = (double *)(ws + L.Uu), *D = (double *)(ws + L.D);
+    double *Ebuf = (double *)(ws + L.Ebuf), *Fbuf = (double *)(ws + L.Fbuf);
+    unsigned long long *cmD = (unsigned long long *)(ws + L.colmax), *cmE = cmD + B, *cmF = cmE + B;
+    unsigned long long *dummy = (unsigned long long *)(ws + J.dummy);
+    SMX_TRY_CUDA(cudaMemsetAsync(cmD, 0, 3 * B * sizeof(unsigned long long), s));
+    auto args = [&](int64_t K, const int32_t *eA, const int32_t *eB, split::Operand &out, int t_shift, double *V,
+                    unsigned long long *cm) {
+        ColArgs a;
+        memset(&a, 0, sizeof(a));
+        a.K = K;
+        a.n_rhs = B;
+        a.T = S.Tacc;
+        a.R = S.Racc;
+        a.eA = eA;
+        a.eB = eB;
+        a.Y = Y;
+        a.E = Ebuf;
+        a.g = S.gdiag;
+        a.Z = Z;
+        a.Uu = Uu;
+        a.D = D;
+        a.V = V;
+        a.colmax = cm;
+        a.reset = dummy;
+        a.coefp = frob + 1;
+        a.colcoef = kcoef;
+        a.w_init = p->w_init;
+        a.slices = out.slices;
+        a.expo = out.expo;
+        a.k_tiles = out.k_tiles;
+        a.slice_elems = out.slice_elems();
+        a.tile_rows = out.tile_rows;
+        a.t_shift = t_shift;
+        return a;
+    };
+    auto slices = [&](const ColArgs &a, const split::Operand &out) {
+        const dim3 g2((unsigned)((out.k_tiles * split::KT + COL_CHUNK - 1) / COL_CHUNK), (unsigned)B);
+        column_slices_kernel<<<g2, COL_CHUNK / 8, 0, s>>>(a);
+        count_launch();
+    };
+    split::Acc acc_m{S.Tacc, S.Racc, m}, acc_n{S.Tacc, S.Racc, n};
+    const int sh_ud = 8 * (split::exact_levels(sh.Ua, sh.Ds) - 1);
+    const int sh_ge = 8 * (split::exact_levels(sh.Xg, sh.Es) - 1);
+    const int sh_uf = 8 * (split::exact_levels(sh.Ut, sh.Fs) - 1);
+    const dim3 gm((unsigned)((m + COL_CHUNK - 1) / COL_CHUNK), (unsigned)B);
+    const dim3 gn((unsigned)((n + COL_CHUNK - 1) / COL_CHUNK), (unsigned)B);
+    {   // z = w_init, u = 0, D = k_j w_init, sliced
+        ColArgs a = args(n, nullptr, nullptr, sh.Ds, 0, D, cmD);
+        column_values_kernel<COL_INIT><<<gn, 256, 0, s>>>(a);
+        count_launch();
+        slices(a, sh.Ds);
+    }
+    for (int it = 0; it < p->maxiter; ++it) {
+        if ((st = split::gemm(sh.Ua, sh.Ds, acc_m, false, S.derr, s, 7))) return st;   // U D
+        SMX_TRY_CUDA(cudaMemsetAsync(cmE, 0, B * sizeof(unsigned long long), s));
+        {
+            ColArgs a = args(m, sh.Ua.expo, sh.Ds.expo, sh.Es, sh_ud, Ebuf, cmE);
+            jk_resid_kernel<<<gm, 256, 0, s>>>(a, rowgrp);                             // E = mask(Y - U D)
+            count_launch();
+            slices(a, sh.Es);
+        }
+        for (int t = 0; t < terms; ++t) {
+            const bool last = t == terms - 1;
+            if ((st = split::gemm(sh.Xg, sh.Es, acc_m, false, S.derr, s))) return st;   // O V
+            jk_dvals_kernel<<<(unsigned)((B + 127) / 128), 128, 0, s>>>(S.Tacc, S.Racc, sh.Xg.expo, sh.Es.expo, sh_ge,
+                                                                        drop, max_drop, B, m, Zinv, cbuf);
+            count_launch();
+            unsigned long long *cm = last ? cmF : cmE;
+            SMX_TRY_CUDA(cudaMemsetAsync(cm, 0, B * sizeof(unsigned long long), s));
+            split::Operand &out = last ? sh.Fs : sh.Es;
+            ColArgs a = args(m, sh.Xg.expo, sh.Es.expo, out, sh_ge, last ? Fbuf : Ebuf, cm);
+            jk_apply_kernel<<<gm, 256, 0, s>>>(a, rowgrp, drop, max_drop, S.Xd, cbuf, mu, Fbuf, t == 0 ? 1 : 0,
+                                               last ? 1 : 0);
+            count_launch();
+            slices(a, out);
+        }
+        if ((st = split::gemm(sh.Ut, sh.Fs, acc_n, false, S.derr, s, 7))) return st;   // U^T F
+        SMX_TRY_CUDA(cudaMemsetAsync(cmD, 0, B * sizeof(unsigned long long), s));
+        {
+            ColArgs a = args(n, sh.Ut.expo, sh.Fs.expo, sh.Ds, sh_uf, D, cmD);
+            column_values_kernel<COL_UPDATE><<<gn, 256, 0, s>>>(a);                     // ADMM update, D
+            count_launch();
+            slices(a, sh.Ds);
+        }
+    }
+    SMX_TRY_CUDA(cudaMemcpyAsync(Z_out, Z, sizeof(double) * n * B, cudaMemcpyDeviceToDevice, s));
+    SMX_TRY_CUDA(cudaGetLastError());
+    int hinfo[4] = {0, 0, 0, 0}, herr = 0;
+    SMX_TRY_CUDA(cudaMemcpyAsync(hinfo, dinfo, sizeof(hinfo), cudaMemcpyDeviceToHost, s));
+    SMX_TRY_CUDA(cudaMemcpyAsync(&herr, S.derr, sizeof(int), cudaMemcpyDeviceToHost, s));
+    SMX_TRY_CUDA(cudaStreamSynchronize(s));
+    if (hinfo[3] != 0) return set_error(SMX_ERR_ARGUMENT, "row_map holds an index outside [0, ld_lib)");
+    if (hinfo[0] != 0) return set_error(SMX_ERR_NUMERIC, "Cholesky of rho' I + U U^T failed (info=%d)", hinfo[0]);
+    if (hinfo[1] != 0) return set_error(SMX_ERR_NUMERIC, "inverse of the Cholesky factor failed (info=%d)", hinfo[1]);
+    if (herr != 0) return set_error(SMX_ERR_CUDA, "split product kernel gave up waiting (code %d)", herr);
+    return SMX_OK;
+}
+
 }  // namespace smx
 
 using namespace smx;
@@ -777,5 +1197,53 @@ extern "C" int smx_nnls_admm(const smx_nnls_problem *p, const void *library, con
         return run<float>(p, (const float *)library, row_map, row_scale, Y, Z_out, (unsigned char *)workspace, L, h, s);
     if (p->lib_precision == SMX_FP64)
         return run<double>(p, (const double *)library, row_map, row_scale, Y, Z_out, (unsigned char *)workspace, L, h, s);
+    return set_error(SMX_ERR_ARGUMENT, "bad library precision %d", p->lib_precision);
+}
+
+extern "C" int smx_nnls_jackknife_workspace_size(const smx_nnls_problem *p, int max_drop, size_t *bytes) {
+    if (!p || !bytes) return set_error(SMX_ERR_ARGUMENT, "smx_nnls_jackknife_workspace_size: NULL argument");
+    if (p->n < 1 || p->m < 1 || p->n_rhs < 1 || max_drop < 1 || max_drop > JK_MAX_DROP)
+        return set_error(SMX_ERR_ARGUMENT, "smx_nnls_jackknife_workspace_size: bad sizes");
+    Handles *h = nullptr;
+    int st = get_handles(nullptr, &h);
+    if (st) return st;
+    smx_nnls_problem q = *p;
+    q.mode = SMX_NNLS_MIXED;
+    Layout L;
+    if ((st = layout(&q, &L, h->solver))) return st;
+    *bytes = jk_layout(L.total, p->m, p->n_rhs, max_drop).total;
+    return SMX_OK;
+}
+
+extern "C" int smx_nnls_jackknife(const smx_nnls_problem *p, const void *library, const int32_t *row_map,
+                                  const double *row_scale, const double *Y, const int32_t *drop_rows, int max_drop,
+                                  double *Z_out, void *workspace, size_t workspace_bytes, void *stream) {
+    if (!p) return set_error(SMX_ERR_ARGUMENT, "smx_nnls_jackknife: problem is NULL");
+    if (p->n < 1 || p->m < 1 || p->n_rhs < 1 || p->maxiter < 0 || p->ld_lib < 1 || max_drop < 1 ||
+        max_drop > JK_MAX_DROP)
+        return set_error(SMX_ERR_ARGUMENT, "smx_nnls_jackknife: bad sizes (1 <= max_drop <= %d)", JK_MAX_DROP);
+    if (p->m > 46340 || p->n * p->m > ((int64_t)1 << 31) * 8 || p->n_rhs > 65535)
+        return set_error(SMX_ERR_UNSUPPORTED, "smx_nnls_jackknife: problem too large");
+    if (p->mode != SMX_NNLS_MIXED)
+        return set_error(SMX_ERR_UNSUPPORTED, "smx_nnls_jackknife: only the mixed mode (SMX_NNLS_MIXED) is batched");
+    if (!library || !row_map || !row_scale || !Y || !drop_rows || !Z_out || !workspace)
+        return set_error(SMX_ERR_ARGUMENT, "smx_nnls_jackknife: NULL buffer");
+    if (!(p->lambda_reg >= 0)) return set_error(SMX_ERR_ARGUMENT, "smx_nnls_jackknife: lambda must be >= 0");
+    cudaStream_t s = (cudaStream_t)stream;
+    Handles *h = nullptr;
+    int st = get_handles(s, &h);
+    if (st) return st;
+    Layout L;
+    if ((st = layout(p, &L, h->solver))) return st;
+    const JkLayout J = jk_layout(L.total, p->m, p->n_rhs, max_drop);
+    if (workspace_bytes < J.total)
+        return set_error(SMX_ERR_WORKSPACE, "smx_nnls_jackknife: workspace %zu < %zu bytes", workspace_bytes, J.total);
+    unsigned char *ws = (unsigned char *)workspace;
+    if (p->lib_precision == SMX_FP32)
+        return run_jackknife<float>(p, (const float *)library, row_map, row_scale, Y, drop_rows, max_drop, Z_out, ws, L,
+                                    J, h, s);
+    if (p->lib_precision == SMX_FP64)
+        return run_jackknife<double>(p, (const double *)library, row_map, row_scale, Y, drop_rows, max_drop, Z_out, ws,
+                                     L, J, h, s);
     return set_error(SMX_ERR_ARGUMENT, "bad library precision %d", p->lib_precision);
 }

@@ -42,10 +42,15 @@ class Settings:
     bulge_mass: float = None
     precision: str = "mixed"         # "mixed" (FP32 orbits, split tensor-core NNLS) or "fp64"
     order_probe: bool = False        # sampled mode: order the orbits by the cost of a one-period probe
+    nnls: str = None                 # "mixed" / "fp64" NNLS independently of the orbits (None: follow precision)
 
     @property
     def dtype(self):
         return torch.float32 if self.precision == "mixed" else torch.float64
+
+    @property
+    def nnls_mixed(self):
+        return (self.nnls or self.precision) == "mixed"
 
     @property
     def slots(self):
@@ -331,7 +336,7 @@ def solve_library(pot, params_disk_rho, dd: DeviceData, grid: Grid, st: Settings
     host = torch.stack([d["y_rz"].sum() / n, d["mmpo"]]).cpu()
     w_init, mmpo = float(host[0]), float(host[1])
     W = kernels.nnls_admm(lib, row_map(nc, nb), row_scale, Y, nnls_maxiter, regularization, w_init,
-                          mixed=st.precision == "mixed")
+                          mixed=st.nnls_mixed)
     y_xy_b, y_h_b, sh_raw = likelihood_data(dd)
     maps, logl = kernels.model_maps(lib, nc, nb, W, d["gamma"].contiguous(), dd.v0, dd.s, d["y_rz"].contiguous(),
                                     dd.xy, y_xy_b, y_h_b, sh_raw, mmpo * d["l2m"], sigma_amplify,

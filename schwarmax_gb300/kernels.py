@@ -237,6 +237,30 @@ def nnls_admm(library, row_map, row_scale, Y, maxiter, lambda_reg, w_init, mixed
     return Z
 
 
+def nnls_jackknife(library, row_map, row_scale, y, drop_rows, maxiter, lambda_reg, w_init):
+    """All leave-group-out replicates of the single right-hand-side NNLS in one batched
+    mixed-precision solve (smx_nnls_jackknife).  y (m,) double scaled data row;
+    drop_rows (G, max_drop) int32 design rows dropped by each replicate (-1 padding).
+    Returns Z (G, n) double."""
+    n, ld = library.shape
+    m = row_map.numel()
+    G, max_drop = drop_rows.shape
+    _check(library, "library", library.dtype, (n, ld))
+    _check(row_map, "row_map", torch.int32, (m,))
+    _check(row_scale, "row_scale", torch.float64, (m,))
+    _check(y, "y", torch.float64, (m,))
+    _check(drop_rows, "drop_rows", torch.int32, (G, max_drop))
+    prob = SmxNnlsProblem(n=n, m=m, n_rhs=G, ld_lib=ld, lib_precision=_prec(library.dtype), mode=_lib.SMX_NNLS_MIXED,
+                          maxiter=int(maxiter), lambda_reg=float(lambda_reg), w_init=float(w_init))
+    nbytes = ctypes.c_size_t(0)
+    call("smx_nnls_jackknife_workspace_size", ctypes.byref(prob), int(max_drop), ctypes.byref(nbytes))
+    ws = _ws.get(nbytes.value, library.device)
+    Z = torch.empty(G, n, dtype=torch.float64, device=library.device)
+    call("smx_nnls_jackknife", ctypes.byref(prob), _ptr(library), _ptr(row_map), _ptr(row_scale), _ptr(y),
+         _ptr(drop_rows), int(max_drop), _ptr(Z), _ptr(ws), ws.numel(), _stream())
+    return Z
+
+
 def split_gemm(A, B, a_slices=4, b_slices=4, lower=False):
     """C = A @ B for double CUDA tensors A (M, K), B (K, N) through the split
     (Ozaki) tensor-core product smx_split_gemm; returns C (M, N) double.

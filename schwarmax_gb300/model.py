@@ -122,6 +122,10 @@ def model_deltaChi2_jackknife(density_func, potential_func, chi2_func, params_ha
     lum = float(d["mmpo"].item()) * d["l2m"]
     rm = engine.row_map(nc, nb)
     grp = torch.arange(nb, device="cuda") % n_groups
+    per_group = -(-nb // int(n_groups))
+    if st.nnls_mixed and 5 * per_group <= 40 and int(n_groups) >= 1:
+        return _jackknife_batched(chi2_func, lib, d, dd, nc, nb, int(n_groups), per_group, rm, w_init, lum,
+                                  nnls_maxiter, regularization)
     chi2 = []
     zeros_b = torch.zeros(1, nb, dtype=torch.float64, device="cuda")
     for g in range(n_groups):
@@ -131,7 +135,7 @@ def model_deltaChi2_jackknife(density_func, potential_func, chi2_func, params_ha
         row_scale, Y = engine.nnls_inputs(d, dd, nc, (math.sqrt(5.0), math.sqrt(5.0), 1.0), boot=False,
                                           sig_xy=sxy, sig_h=sh)
         W = kernels.nnls_admm(lib, rm, row_scale, Y, nnls_maxiter, regularization, w_init,
-                              mixed=st.precision == "mixed")
+                              mixed=st.nnls_mixed)
         maps, _ = kernels.model_maps(lib, nc, nb, W, d["gamma"].contiguous(), dd.v0, dd.s, d["y_rz"].contiguous(),
                                      dd.xy, (dd.xy[None] + zeros_b).contiguous(),
                                      (dd.h[:, None, :]).contiguous(), (dd.h_err + 1e-12).contiguous(), lum)
@@ -140,4 +144,42 @@ def model_deltaChi2_jackknife(density_func, potential_func, chi2_func, params_ha
                               m["surface_density"][0], sxy * lum, dd.h[0], m["h1"][0], sh[0], dd.h[1], m["h2"][0],
                               sh[1], dd.h[2], m["h3"][0], sh[2], dd.h[3], m["h4"][0], sh[3]))
     c = torch.stack([torch.as_tensor(v, dtype=torch.float64, device="cuda") for v in chi2])
+    return torch.std(c, unbiased=False)
+
+
+def _jackknife_batched(chi2_func, lib, d, dd, nc, nb, n_groups, per_group, rm, w_init, lum, maxiter, lam):
+    """All replicates in one batched solve (smx_nnls_jackknife): replicate g drops the
+    design rows (xy, h1..h4) of the bins with bin % n_groups == g; the model maps of
+    every replicate come from one product, and chi2_func is applied per replicate with
+    the reference's masked sigmas (1e20 on the dropped bins)."""
+    from .likelihood import chi2_func as canonical_chi2
+    bins = torch.arange(nb, device="cuda")
+    drop = torch.full((n_groups, 5 * per_group), -1, dtype=torch.int32, device="cuda")
+    for q in range(per_group):
+        b = torch.arange(n_groups, device="cuda") + q * n_groups
+        ok = b < nb
+        for k in range(5):
+            drop[:, 5 * q + k] = torch.where(ok, nc + k * nb + b, torch.full_like(b, -1)).to(torch.int32)
+    row_scale, Y = engine.nnls_inputs(d, dd, nc, (math.sqrt(5.0), math.sqrt(5.0), 1.0), boot=False)
+    W = kernels.nnls_jackknife(lib, rm, row_scale, Y[0].contiguous(), drop.contiguous(), maxiter, lam, w_init)
+    G = n_groups
+    y_xy_b = dd.xy[None].expand(G, nb).contiguous()
+    y_h_b = dd.h[:, None, :].expand(4, G, nb).contiguous()
+    maps, _ = kernels.model_maps(lib, nc, nb, W, d["gamma"].contiguous(), dd.v0, dd.s, d["y_rz"].contiguous(), dd.xy,
+                                 y_xy_b, y_h_b, (dd.h_err + 1e-12).contiguous(), lum)
+    m = split_maps(maps, nc, nb)
+    dropped = (bins[None, :] % n_groups) == torch.arange(G, device="cuda")[:, None]     # (G, nb)
+    sh = torch.where(dropped[None], torch.full((4, G, nb), 1e20, dtype=torch.float64, device="cuda"),
+                     d["sh"][:, None, :].expand(4, G, nb))
+    if chi2_func is canonical_chi2:
+        r = sum(torch.nansum(((dd.h[k][None] - m[f"h{k + 1}"]) / sh[k]) ** 2, dim=1) for k in range(4))
+        c = -0.5 * r
+    else:
+        sxy = torch.where(dropped, torch.full((G, nb), 1e20, dtype=torch.float64, device="cuda"),
+                          d["sig_xy"][None].expand(G, nb))
+        c = torch.stack([torch.as_tensor(chi2_func(d["y_rz"], m["density_3d_model"][j], d["sig_rz"], d["y_xy"] * lum,
+                                                   m["surface_density"][j], sxy[j] * lum, dd.h[0], m["h1"][j], sh[0, j],
+                                                   dd.h[1], m["h2"][j], sh[1, j], dd.h[2], m["h3"][j], sh[2, j],
+                                                   dd.h[3], m["h4"][j], sh[3, j]), dtype=torch.float64,
+                                         device="cuda") for j in range(G)])
     return torch.std(c, unbiased=False)

@@ -12,8 +12,9 @@ Each case is small enough for a pure-Python run and is written to
 draw the reference made (jax.random draws are logged by the shim), so that the
 oracle can be replayed on the same numbers.
 
-Usage:  python tests/golden/make_golden.py [REF]     (REF defaults to the
-reference checkout path given on the command line or /root/reference)
+Usage:  python tests/golden/make_golden.py REF [case ...]
+REF is the path of the reference checkout (required); the cases default to the
+list at the end of this file.
 """
 import math
 import os
@@ -23,7 +24,9 @@ import time
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) < 2 or not os.path.isdir(sys.argv[1]):
+    sys.exit("usage: python tests/golden/make_golden.py REF [case ...]   (REF: the reference checkout)")
+REF = sys.argv[1]
 sys.path[:0] = [os.path.join(HERE, "jaxshim"), REF]
 
 import jax  # noqa: E402  (the shim)
@@ -406,6 +409,25 @@ def case_example_jackknife():
     dchi2 = float(likelihood.calculate_delta_chi2(g["theta"], d, d["total_bins"], d["Rzphi_n_tot"]))
     print(f"  calculate_delta_chi2: {time.time() - t0:.1f}s  dchi2={dchi2}")
     save("example_jackknife", theta=g["theta"], delta_chi2=np.array(dchi2))
+
+
+def case_analysis():
+    """build_Lcirc_of_E (utils.py:275-341) of the canonical potential on a 400-point
+    table with its interpolator at a set of energies, and compute_transfer_matrix
+    (utils.py:413-485) on the example galaxy's 609 apertures (60 x 40 pixels) on a
+    150 x 150 fine grid with a 0.3 kpc PSF."""
+    pb, ph = params_pair()
+    interp, E, L = utils.build_Lcirc_of_E(likelihood.potential_func, (pb, ph), R_min=1e-2, R_max=1e2, n_grid=400)
+    rng = np.random.default_rng(5)
+    Eq = np.concatenate([rng.uniform(E[0], E[-1], 300), E[[0, 7, 100, -1]], [E[0] - 10.0, E[-1] + 10.0]])
+    Lq = np.asarray(interp(Eq))
+    g = np.load(os.path.join(OUT, "example_data.npz"))
+    bm = g["out_bin_mapping"]
+    nX, nY = (int(v) for v in g["out_nX_nY"])
+    P = utils.compute_transfer_matrix(0.3, nX, nY, g["out_X_minmax"], g["out_Y_minmax"], bm, int(g["out_total_bins"]),
+                                      grid_res=150)
+    save("analysis", params=flat_params(pb, ph), E_circ=E, L_circ=L, E_query=Eq, L_query=Lq, psf_sigma=np.array(0.3),
+         psf_grid_res=np.array(150), psf_P=P)
 
 
 if __name__ == "__main__":

@@ -114,3 +114,68 @@ def test_mixed_solver_chi2_at_benchmark_width():
     dchi2 = (2 * (logl_m - logl_64)).abs()
     assert float(dchi2.max()) <= 0.05, float(dchi2.max())
     assert float((r["W"] - W64).abs().max() / W64.abs().max()) <= 1e-6
+
+
+@pytest.mark.parametrize("n_groups", [12, 5])
+def test_batched_jackknife_matches_per_replicate_solves(small, n_groups):
+    """smx_nnls_jackknife (every replicate from the one G^-1 of the full problem:
+    Schur complement of the dropped rows, Neumann series for the shift of rho) against
+    one FP64 smx_nnls_admm per replicate with the reference's 1e20 sigma masks, on
+    the same library."""
+    from schwarmax_gb300 import engine, kernels
+    from schwarmax_gb300.likelihood import grid_of, unpack_params
+    from schwarmax_gb300.potentials import potential_struct
+    cfg, dd, thetas = small
+    st = cfg.settings("fp64")
+    halo, bary = unpack_params(thetas[0])
+    pot = potential_struct(bary, halo, st.bulge_mass)
+    ddv = engine.DeviceData(dd, n_real=st.n_real)
+    grid = grid_of(dd)
+    lib = engine.build_library(pot, bary, ddv, grid, st)["library"]
+    nc, nb = grid.n_cells, cfg.n_bins
+    y_rz = kernels.density_target(pot, torch.float64, ddv.R_grid, ddv.z_grid, ddv.phi_grid, ddv.dR, ddv.dz, ddv.dphi,
+                                  ddv.sample)
+    d = engine.data_terms(ddv, bary, y_rz, lib.shape[0])
+    w_init = float((d["y_rz"].sum() / lib.shape[0]).item())
+    rm = engine.row_map(nc, nb)
+    w = (math.sqrt(5.0), math.sqrt(5.0), 1.0)
+    per = -(-nb // n_groups)
+    drop = -np.ones((n_groups, 5 * per), dtype=np.int32)
+    for g in range(n_groups):
+        bins = np.arange(g, nb, n_groups)
+        rows = [nc + k * nb + b for b in bins for k in range(5)]
+        drop[g, :len(rows)] = rows
+    rs, Y = engine.nnls_inputs(d, ddv, nc, w, boot=False)
+    Wb = kernels.nnls_jackknife(lib, rm, rs, Y[0].contiguous(), torch.as_tensor(drop, device="cuda"), 150, 1.0, w_init)
+    grp = torch.arange(nb, device="cuda") % n_groups
+    for g in range(n_groups):
+        m = grp == g
+        sxy = torch.where(m, torch.full_like(d["sig_xy"], 1e20), d["sig_xy"])
+        sh = torch.where(m[None], torch.full_like(d["sh"], 1e20), d["sh"])
+        rsg, Yg = engine.nnls_inputs(d, ddv, nc, w, boot=False, sig_xy=sxy, sig_h=sh)
+        Wg = kernels.nnls_admm(lib, rm, rsg, Yg, 150, 1.0, w_init, mixed=False)[0]
+        scale = float(Wg.abs().max())
+        assert float((Wb[g] - Wg).abs().max()) <= 1e-6 * scale, g
+
+
+def test_calculate_delta_chi2_batched_matches_loop(small):
+    """calculate_delta_chi2 in mixed precision (batched replicates) against the FP64
+    per-replicate loop on the same FP64 library."""
+    from schwarmax_gb300 import model
+    from schwarmax_gb300.likelihood import chi2_func, grid_of, unpack_params
+    from schwarmax_gb300.potentials import density_func, potential_func
+    cfg, dd, thetas = small
+    halo, bary = unpack_params(thetas[1])
+    grid = grid_of(dd)
+    nc = grid.n_cells
+    kw = dict(Rzphi_n_grid=grid.n_rzphi, Rzphi_lim_grid=grid.rzphi_lim, xy_lim_grid=grid.xy_lim, xy_n_grid=grid.n_xy,
+              nnls_maxiter=120, n_groups=cfg.n_bins)
+    st64 = cfg.settings("fp64")
+    ref = model.model_deltaChi2_jackknife(density_func, potential_func, chi2_func, halo, bary, dd, cfg.n_bins, nc,
+                                          settings=st64, **kw)
+    # the batched path on the same FP64 library: FP64 orbits, mixed NNLS
+    st_b = cfg.settings("fp64")
+    st_b.nnls = "mixed"
+    got = model.model_deltaChi2_jackknife(density_func, potential_func, chi2_func, halo, bary, dd, cfg.n_bins, nc,
+                                          settings=st_b, **kw)
+    assert abs(float(got) - float(ref)) <= 1e-6 * abs(float(ref)) + 1e-9, (float(got), float(ref))
