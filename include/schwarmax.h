@@ -337,6 +337,16 @@ int smx_split_gemm_workspace_size(int64_t M, int64_t N, int64_t K, int a_slices,
 int smx_split_gemm(int64_t M, int64_t N, int64_t K, int a_slices, int b_slices, int lower, const double *A,
                    const double *B, double *C, void *workspace, size_t workspace_bytes, void *stream);
 
+/* FP32 inverse of a symmetric positive definite m x m matrix G (column-major
+ * double input, float output Xinv (m x m)) by blocked Gauss-Jordan elimination
+ * without pivoting, 2 m^3 flops on the FP32 pipe.  It is the seed that the mixed
+ * NNLS refines by Newton-Schulz steps to FP64 accuracy (in place of the reference's
+ * Cholesky factorisation, nnls.py:121); exposed so that it can be tested on its own.
+ * Returns SMX_ERR_NUMERIC when a pivot is not positive.  Synchronises the stream. */
+int smx_spd_inverse_f32_workspace_size(int64_t m, size_t *bytes);
+int smx_spd_inverse_f32(const double *G, int64_t m, float *Xinv, void *workspace, size_t workspace_bytes,
+                        void *stream);
+
 /* ------------------------------------------------------- model maps, chi2 */
 typedef struct {
     int64_t n;           /* orbits */
@@ -415,6 +425,25 @@ int smx_psf_transfer_workspace_size(int grid_res, int total_bins, int radius, si
 int smx_psf_transfer(const double *kernel_weights, int radius, int nX, int nY, double X_lo, double X_hi, double Y_lo,
                      double Y_hi, const int32_t *bin_mapping, int total_bins, int grid_res, double *P, void *workspace,
                      size_t workspace_bytes, void *stream);
+
+/* ---------------------------------------------------- MCMC driver (RMH step) */
+/* One random-walk Metropolis-Hastings step of n_chains chains in ndim dimensions
+ * on the device (the reference's BlackJAX additive random walk with a normal
+ * proposal and a uniform box prior, example/example_schwarmax.ipynb cell 12), in
+ * two halves around the batched likelihood of the proposals:
+ *   smx_rmh_propose: x_prop = x + L eps (L (ndim, ndim) lower triangular row-major,
+ *     eps (n_chains, ndim) standard normals), logprior = -log_vol inside
+ *     [lo, hi], -inf outside;
+ *   smx_rmh_accept: with lp' = logprior_prop + loglike_prop (a non-finite
+ *     log-likelihood counts as -1e30), accept where u < min(1, exp(lp' - logdensity))
+ *     (u (n_chains) uniform draws): x and logdensity are updated in place and
+ *     accepted (n_chains) int32 records the decision.
+ * All arrays double (int32 for accepted) on the device; draws are inputs. */
+int smx_rmh_propose(const double *x, const double *L, const double *eps, int n_chains, int ndim, const double *lo,
+                    const double *hi, double log_vol, double *x_prop, double *logprior, void *stream);
+int smx_rmh_accept(double *x, double *logdensity, const double *x_prop, const double *logprior_prop,
+                   const double *loglike_prop, const double *u, int n_chains, int ndim, int32_t *accepted,
+                   void *stream);
 
 #ifdef __cplusplus
 }

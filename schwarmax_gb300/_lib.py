@@ -19,7 +19,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(HERE, "libschwarmax_gb300.so")
 SOURCES = ["api.cu", "pointkernels.cu", "integrate.cu", "project_bin.cu", "soft_project.cu", "nnls.cu", "split_gemm.cu",
-           "maps.cu", "analysis.cu"]
+           "maps.cu", "analysis.cu", "spd_inverse.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 SMX_FP32, SMX_FP64 = 0, 1
@@ -33,7 +33,8 @@ EXPORTS = ["smx_version", "smx_kernel_launches", "smx_status_string", "smx_last_
            "smx_sample_cells", "smx_soft_project", "smx_soft_project_adjoint", "smx_nnls_workspace_size",
            "smx_nnls_admm", "smx_nnls_jackknife_workspace_size", "smx_nnls_jackknife", "smx_split_gemm_workspace_size",
            "smx_split_gemm", "smx_model_maps", "smx_model_maps_workspace_size", "smx_lcirc_table", "smx_spline_eval",
-           "smx_circularity", "smx_histogram2d", "smx_psf_transfer_workspace_size", "smx_psf_transfer"]
+           "smx_circularity", "smx_histogram2d", "smx_psf_transfer_workspace_size", "smx_psf_transfer",
+           "smx_rmh_propose", "smx_rmh_accept", "smx_spd_inverse_f32_workspace_size", "smx_spd_inverse_f32"]
 
 
 class SmxError(RuntimeError):
@@ -173,6 +174,10 @@ _SIGS = {
     "smx_psf_transfer": ([_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                           ctypes.c_double, ctypes.c_double, _P, ctypes.c_int, ctypes.c_int, _P, _P, ctypes.c_size_t,
                           _P], ctypes.c_int),
+    "smx_rmh_propose": ([_P, _P, _P, ctypes.c_int, ctypes.c_int, _P, _P, ctypes.c_double, _P, _P, _P], ctypes.c_int),
+    "smx_rmh_accept": ([_P, _P, _P, _P, _P, _P, ctypes.c_int, ctypes.c_int, _P, _P], ctypes.c_int),
+    "smx_spd_inverse_f32_workspace_size": ([_I64, ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
+    "smx_spd_inverse_f32": ([_P, _I64, _P, _P, ctypes.c_size_t, _P], ctypes.c_int),
     "smx_split_gemm_workspace_size": ([ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int, ctypes.c_int,
                                        ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
     "smx_split_gemm": ([ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P,

@@ -348,3 +348,72 @@ extern "C" int smx_psf_transfer(const double *kernel_weights, int radius, int nX
                          PSF_MAX_BINS);
     return SMX_OK;
 }
+
+// ---------------------------------------------------------------- MCMC (RMH)
+namespace smx {
+
+// Random-walk Metropolis-Hastings proposal of every chain (the additive normal
+// random walk of the reference's sampler, example/example_schwarmax.ipynb cell 12):
+//   x' = x + L eps  (L lower triangular, row-major D x D), and the uniform prior's
+//   log density: -sum log(hi - lo) inside the box, -inf outside.
+__global__ void rmh_propose_kernel(const double *__restrict__ x, const double *__restrict__ L,
+                                   const double *__restrict__ eps, int C, int D, const double *__restrict__ lo,
+                                   const double *__restrict__ hi, double log_vol, double *xp, double *logprior) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= C) return;
+    bool in = true;
+    for (int i = 0; i < D; ++i) {
+        double s = x[c * D + i];
+        for (int j = 0; j <= i; ++j) s += L[i * D + j] * eps[c * D + j];
+        xp[c * D + i] = s;
+        in = in && (s >= lo[i]) && (s <= hi[i]);
+    }
+    logprior[c] = in ? -log_vol : -INFINITY;
+}
+
+// Metropolis acceptance with the symmetric proposal: accept with probability
+// min(1, exp(lp' - lp)) (u < p), the log-likelihood of a proposal replaced by -1e30
+// when it is not finite (as the reference's logdensity_fn does).
+__global__ void rmh_accept_kernel(double *x, double *lp, const double *__restrict__ xp,
+                                  const double *__restrict__ logprior_p, const double *__restrict__ ll_p,
+                                  const double *__restrict__ u, int C, int D, int32_t *accepted) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= C) return;
+    const double ll = ll_p[c];
+    const double lpn = logprior_p[c] + (isfinite(ll) ? ll : -1e30);
+    const double d = lpn - lp[c];
+    const double p = d >= 0 ? 1.0 : exp(d);
+    const bool acc = u[c] < p;
+    if (acc) {
+        for (int i = 0; i < D; ++i) x[c * D + i] = xp[c * D + i];
+        lp[c] = lpn;
+    }
+    accepted[c] = acc ? 1 : 0;
+}
+
+}  // namespace smx
+
+extern "C" int smx_rmh_propose(const double *x, const double *L, const double *eps, int n_chains, int ndim,
+                               const double *lo, const double *hi, double log_vol, double *x_prop, double *logprior,
+                               void *stream) {
+    if (n_chains < 1 || ndim < 1 || !x || !L || !eps || !lo || !hi || !x_prop || !logprior)
+        return set_error(SMX_ERR_ARGUMENT, "smx_rmh_propose: bad arguments");
+    rmh_propose_kernel<<<blocks_for(n_chains, 64), 64, 0, (cudaStream_t)stream>>>(x, L, eps, n_chains, ndim, lo, hi,
+                                                                                 log_vol, x_prop, logprior);
+    count_launch();
+    SMX_TRY_CUDA(cudaGetLastError());
+    return SMX_OK;
+}
+
+extern "C" int smx_rmh_accept(double *x, double *logdensity, const double *x_prop, const double *logprior_prop,
+                              const double *loglike_prop, const double *u, int n_chains, int ndim, int32_t *accepted,
+                              void *stream) {
+    if (n_chains < 1 || ndim < 1 || !x || !logdensity || !x_prop || !logprior_prop || !loglike_prop || !u || !accepted)
+        return set_error(SMX_ERR_ARGUMENT, "smx_rmh_accept: bad arguments");
+    rmh_accept_kernel<<<blocks_for(n_chains, 64), 64, 0, (cudaStream_t)stream>>>(x, logdensity, x_prop, logprior_prop,
+                                                                                loglike_prop, u, n_chains, ndim,
+                                                                                accepted);
+    count_launch();
+    SMX_TRY_CUDA(cudaGetLastError());
+    return SMX_OK;
+}

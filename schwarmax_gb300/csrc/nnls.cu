@@ -41,6 +41,12 @@
 
 namespace smx {
 
+// FP32 SPD inverse by blocked Gauss-Jordan (spd_inverse.cu)
+int64_t spd_inverse_padded(int64_t m);
+size_t spd_inverse_workspace(int64_t m);
+int spd_inverse_inplace(float *Ap, int64_t mp, float *ws, int *flag, cudaStream_t s);
+__global__ void gj_pad_kernel(const double *__restrict__ G, int64_t m, float *Ap, int64_t mp);
+
 struct Handles {
     cublasHandle_t blas = nullptr;
     cusolverDnHandle_t solver = nullptr;
@@ -110,7 +116,7 @@ struct Layout {
     // split path
     size_t Tacc, Racc, rowmax, err;
     size_t Ua, Ua_e, Ut, Ut_e, Xg, Xg_e, Ds, Ds_e, Es, Es_e, Fs, Fs_e;
-    size_t G7, G7_e, X7, X7_e, X5, X5_e, R5, R5_e, Gf, Xd, Rd, Ebuf, Fbuf, gdiag, colmax;
+    size_t G7, G7_e, X7, X7_e, X5, X5_e, R5, R5_e, Gf, gjws, nsflag, Xd, Rd, Ebuf, Fbuf, gdiag, colmax;
     int lwork_s;   // float Cholesky / inverse scratch (floats)
     int64_t acc_elems;
     size_t work_bytes, host_bytes;   // device / host scratch of the factorisation and inversion
@@ -129,16 +135,13 @@ static int layout(const smx_nnls_problem *p, Layout *L, cusolverDnHandle_t solve
     if (solver) {
         if (!mixed) {
             SMX_TRY_SOLVER(cusolverDnDpotrf_bufferSize(solver, CUBLAS_FILL_MODE_LOWER, (int)m, nullptr, (int)m, &lwork));
-        } else {
-            SMX_TRY_SOLVER(cusolverDnSpotrf_bufferSize(solver, CUBLAS_FILL_MODE_LOWER, (int)m, nullptr, (int)m, &lw_f));
-            SMX_TRY_SOLVER(cusolverDnSpotri_bufferSize(solver, CUBLAS_FILL_MODE_LOWER, (int)m, nullptr, (int)m, &lw_i));
         }
     } else {
         lwork = lw_f = lw_i = (int)(m * 256 + (1 << 20));   // generous estimate for size queries without a handle
     }
     L->lwork = lwork;
     L->lwork_s = lw_f > lw_i ? lw_f : lw_i;
-    L->work_bytes = mixed ? (size_t)L->lwork_s * sizeof(float) : (size_t)lwork * sizeof(double);
+    L->work_bytes = mixed ? 256 : (size_t)lwork * sizeof(double);
     L->host_bytes = 0;
     L->work = take(L->work_bytes);
     L->info = take(sizeof(int) * 4);
@@ -171,7 +174,10 @@ static int layout(const smx_nnls_problem *p, Layout *L, cusolverDnHandle_t solve
         op(sh.X7, L->X7, L->X7_e);
         op(sh.X5, L->X5, L->X5_e);
         op(sh.R5, L->R5, L->R5_e);
-        L->Gf = take(m * m * sizeof(float));
+        const int64_t mp = spd_inverse_padded((int64_t)m);
+        L->Gf = take((size_t)mp * mp * sizeof(float));      // padded float copy of G, inverted in place
+        L->gjws = take(spd_inverse_workspace((int64_t)m));
+        L->nsflag = take(16 * sizeof(int));
         L->Xd = take(m * m * sizeof(double));
         L->Rd = take(m * m * sizeof(double));
         L->Ebuf = take(m * B * sizeof(double));
@@ -285,6 +291,8 @@ __device__ __forceinline__ double product_value(const unsigned long long *T, con
 }
 
 enum { COL_INIT = 0, COL_RESID = 1, COL_PLAIN = 2, COL_UPDATE = 3 };
+
+constexpr int kNsMaxSteps = 5;   // Newton-Schulz steps at most (a seed residual of 0.2 needs 4)
 
 constexpr int VS = 5;          // slices of the vector operands: 39 bits below each column's largest magnitude
 constexpr int COL_CHUNK = 1024;   // k per CTA of the column kernels
@@ -435,7 +443,7 @@ __global__ void __launch_bounds__(COL_CHUNK / 8) column_slices_kernel(const ColA
 // Gram combine: G = 2^(e_r + e_c - 14)(T/256 + R) + c I from the lower-triangle
 // product tiles, written to both triangles in double and to a float copy for the
 // seed factorisation; T and R are cleared for the next product.
-__global__ void gram_combine_kernel(unsigned long long *T, float *R, const int32_t *e, double *G, float *Gf, int64_t m,
+__global__ void gram_combine_kernel(unsigned long long *T, float *R, const int32_t *e, double *G, int64_t m,
                                     const double *frob, double lambda, double n) {
     const double c = (frob[0] + lambda) / n + lambda / n;
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < m * m; k += (int64_t)gridDim.x * blockDim.x) {
@@ -445,19 +453,48 @@ __global__ void gram_combine_kernel(unsigned long long *T, float *R, const int32
             if (r == col) v += c;
             G[k] = v;
             G[col + m * r] = v;
-            Gf[k] = (float)v;
         }
         T[k] = 0ull;
         R[k] = 0.0f;
     }
 }
 
-// Newton-Schulz seed: X0 = the float inverse (lower triangle of Gf) mirrored, in double
-__global__ void seed_kernel(const float *Gf, double *X, int64_t m) {
+// Newton-Schulz seed: X0 = the symmetric part of the float inverse (padded, leading
+// dimension mp), in double
+__global__ void seed_kernel(const float *Gp, int64_t mp, double *X, int64_t m) {
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < m * m; k += (int64_t)gridDim.x * blockDim.x) {
         const int64_t r = k % m, col = k / m;
-        X[k] = (double)(r >= col ? Gf[k] : Gf[col + m * r]);
+        X[k] = 0.5 * ((double)Gp[r + mp * col] + (double)Gp[col + mp * r]);
     }
+}
+
+// Device-side control of the Newton-Schulz steps (no host read-back): flag[0] = 1
+// while steps are still to run; after the residual of a step, with ss = ||I - G X||_F^2
+// of the step's input: a step whose input is below thr2 is the last one; an input at
+// or above 1/4 (not converging) stops the iteration with flag[1] = 1; flag[2] = 1
+// once a step with a converged input has run.  skip = flag[3] = !flag[0] for the
+// kernels of the next step.
+__global__ void ns_gate_kernel(const double *rss, double thr2, int *flag) {
+    if (!flag[0]) return;
+    const double ss = rss[0];
+    if (!(ss < 0.25)) {
+        flag[0] = 0;
+        flag[1] = 1;
+    } else if (ss <= thr2) {
+        flag[0] = 0;
+        flag[2] = 1;
+    }
+}
+__global__ void ns_skip_kernel(int *flag) { flag[3] = flag[0] ? 0 : 1; }
+__global__ void ns_init_kernel(int *flag) {
+    flag[0] = 1;
+    flag[1] = 0;
+    flag[2] = 0;
+    flag[3] = 0;
+}
+// final verdict of the set-up: dinfo[1] = 1 when the inverse did not converge
+__global__ void ns_verdict_kernel(const int *flag, int *dinfo) {
+    if (flag[1] || !flag[2]) dinfo[1] = 1;
 }
 
 // residual R = I - G X of a Newton-Schulz step.  G and X are dominated by their
@@ -466,7 +503,9 @@ __global__ void seed_kernel(const float *Gf, double *X, int64_t m) {
 // the split product (four exact levels, T in units of 2^-24).  rss receives
 // sum R_ij^2 (||R||_F^2, a bound on ||R||_2^2).
 __global__ void ns_residual_kernel(unsigned long long *T, float *Racc, const int32_t *eG, const int32_t *eX,
-                                   const double *G, const double *X, double *Rd, int64_t m, double *rss) {
+                                   const double *G, const double *X, double *Rd, int64_t m, double *rss,
+                                   const int *skip) {
+    if (*skip) return;
     double acc = 0;
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < m * m; k += (int64_t)gridDim.x * blockDim.x) {
         const int64_t r = k % m, col = k / m;
@@ -486,7 +525,8 @@ __global__ void ns_residual_kernel(unsigned long long *T, float *Racc, const int
 
 // X <- X + X R
 __global__ void ns_update_kernel(unsigned long long *T, float *Racc, const int32_t *eX, const int32_t *eR, double *X,
-                                 int64_t m) {
+                                 int64_t m, const int *skip) {
+    if (*skip) return;
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < m * m; k += (int64_t)gridDim.x * blockDim.x) {
         const int64_t r = k % m, col = k / m;
         X[k] += product_value(T, Racc, k, eX[r], eR[col]);
@@ -581,48 +621,47 @@ static int mixed_setup(const smx_nnls_problem *p, const TL *lib, const int32_t *
     if ((st = split::slice_rows<double>(U, m, 1, sh.Ut, rowmax, s))) return st;
     // G = U U^T + c I from the sliced U (31 bits below each row's largest entry), all slice pairs
     split::Acc acc{Tacc, Racc, m};
-    float *Gf = (float *)(ws + L.Gf);
+    float *Gp = (float *)(ws + L.Gf);
     double *Xd = (double *)(ws + L.Xd), *Rd = (double *)(ws + L.Rd);
     if ((st = split::gemm(sh.Ua, sh.Ua, acc, true, derr, s))) return st;
-    gram_combine_kernel<<<grid1d(m * m), 256, 0, s>>>(Tacc, Racc, sh.Ua.expo, G, Gf, m, frob, lam, (double)n);
+    gram_combine_kernel<<<grid1d(m * m), 256, 0, s>>>(Tacc, Racc, sh.Ua.expo, G, m, frob, lam, (double)n);
     count_launch();
-    // G^-1: float Cholesky inverse as the seed, then Newton-Schulz steps
+    // G^-1: an FP32 inverse (blocked Gauss-Jordan) as the seed, then Newton-Schulz steps
     //   R = I - G X (diagonals exact, off-diagonal parts as a 7 x 7 split
     //   product), X <- X + X R.
     // The new X has residual R^2, whose 2-norm is at most ||R||_F^2: steps
     // continue until a step's input has ||R||_F <= 3e-7, so the result has
     // ||I - G X|| <= 1e-13 up to the accuracy of G X times cond(G) (about 2^-44).
-    SMX_TRY_SOLVER(cusolverDnSpotrf(h->solver, CUBLAS_FILL_MODE_LOWER, (int)m, Gf, (int)m, (float *)(ws + L.work),
-                                    L.lwork_s, dinfo));
-    SMX_TRY_SOLVER(cusolverDnSpotri(h->solver, CUBLAS_FILL_MODE_LOWER, (int)m, Gf, (int)m, (float *)(ws + L.work),
-                                    L.lwork_s, dinfo + 1));
-    seed_kernel<<<grid1d(m * m), 256, 0, s>>>(Gf, Xd, m);
+    // The stopping rule runs on the device (ns_gate_kernel): the kernels of a step
+    // that is not needed return at once, and nothing is read back here.
+    const int64_t mp = spd_inverse_padded(m);
+    int *nsf = (int *)(ws + L.nsflag);
+    gj_pad_kernel<<<4864, 256, 0, s>>>(G, m, Gp, mp);
+    count_launch();
+    if ((st = spd_inverse_inplace(Gp, mp, (float *)(ws + L.gjws), dinfo + 1, s))) return st;
+    seed_kernel<<<grid1d(m * m), 256, 0, s>>>(Gp, mp, Xd, m);
     count_launch();
     if ((st = split::slice_rows<double>(G, 1, m, sh.G7, rowmax, s, true))) return st;   // O_G
     double *rss = frob + 3;
-    double fro = 1.0;
-    for (int steps = 0; steps < 6 && fro > 3e-7; ++steps) {
-        if ((st = split::slice_rows<double>(Xd, m, 1, sh.X7, rowmax, s, true))) return st;   // O_X columns over k
-        if ((st = split::gemm(sh.G7, sh.X7, acc, false, derr, s))) return st;
+    ns_init_kernel<<<1, 1, 0, s>>>(nsf);
+    count_launch();
+    const int *skip = nsf + 3;
+    for (int step = 0; step < kNsMaxSteps; ++step) {
+        if ((st = split::slice_rows<double>(Xd, m, 1, sh.X7, rowmax, s, true, skip))) return st;   // O_X columns over k
+        if ((st = split::gemm(sh.G7, sh.X7, acc, false, derr, s, 0, skip))) return st;
         SMX_TRY_CUDA(cudaMemsetAsync(rss, 0, sizeof(double), s));
-        ns_residual_kernel<<<grid1d(m * m), 256, 0, s>>>(Tacc, Racc, sh.G7.expo, sh.X7.expo, G, Xd, Rd, m, rss);
-        count_launch();
-        if ((st = split::slice_rows<double>(Xd, 1, m, sh.X5, rowmax, s))) return st;   // X rows over k
-        if ((st = split::slice_rows<double>(Rd, m, 1, sh.R5, rowmax, s))) return st;   // R columns over k
-        if ((st = split::gemm(sh.X5, sh.R5, acc, false, derr, s))) return st;
-        ns_update_kernel<<<grid1d(m * m), 256, 0, s>>>(Tacc, Racc, sh.X5.expo, sh.R5.expo, Xd, m);
-        count_launch();
-        double ss = 0;
-        SMX_TRY_CUDA(cudaMemcpyAsync(&ss, rss, sizeof(ss), cudaMemcpyDeviceToHost, s));
-        SMX_TRY_CUDA(cudaStreamSynchronize(s));
-        fro = sqrt(ss);
-        if (!(fro < 0.5)) break;   // not converging: the seed is too far off
+        ns_residual_kernel<<<grid1d(m * m), 256, 0, s>>>(Tacc, Racc, sh.G7.expo, sh.X7.expo, G, Xd, Rd, m, rss, skip);
+        ns_gate_kernel<<<1, 1, 0, s>>>(rss, 9e-14, nsf);
+        count_launch(2);
+        if ((st = split::slice_rows<double>(Xd, 1, m, sh.X5, rowmax, s, false, skip))) return st;   // X rows over k
+        if ((st = split::slice_rows<double>(Rd, m, 1, sh.R5, rowmax, s, false, skip))) return st;   // R columns over k
+        if ((st = split::gemm(sh.X5, sh.R5, acc, false, derr, s, 0, skip))) return st;
+        ns_update_kernel<<<grid1d(m * m), 256, 0, s>>>(Tacc, Racc, sh.X5.expo, sh.R5.expo, Xd, m, skip);
+        ns_skip_kernel<<<1, 1, 0, s>>>(nsf);
+        count_launch(2);
     }
-    if (!(fro <= 3e-7)) {
-        SMX_TRY_CUDA(cudaStreamSynchronize(s));
-        return set_error(SMX_ERR_NUMERIC, "Newton-Schulz inverse of rho' I + U U^T did not converge (||I - G X||_F %g)",
-                         fro);
-    }
+    ns_verdict_kernel<<<1, 1, 0, s>>>(nsf, dinfo);
+    count_launch();
     double *gdiag = (double *)(ws + L.gdiag);
     split_diag_kernel<<<grid1d(m), 256, 0, s>>>(Xd, gdiag, m);
     count_launch();
@@ -771,7 +810,9 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
     SMX_TRY_CUDA(cudaStreamSynchronize(s));
     if (hinfo[3] != 0) return set_error(SMX_ERR_ARGUMENT, "row_map holds an index outside [0, ld_lib)");
     if (hinfo[0] != 0) return set_error(SMX_ERR_NUMERIC, "Cholesky of rho' I + U U^T failed (info=%d)", hinfo[0]);
-    if (mixed && hinfo[1] != 0) return set_error(SMX_ERR_NUMERIC, "inverse of the Cholesky factor failed (info=%d)", hinfo[1]);
+    if (mixed && hinfo[1] != 0)
+        return set_error(SMX_ERR_NUMERIC, "inverse of rho' I + U U^T failed: a non-positive pivot of the FP32 seed or "
+                         "Newton-Schulz steps that do not converge");
     if (mixed && hinfo[2] != 0) return set_error(SMX_ERR_CUDA, "split product kernel gave up waiting (code %d)", hinfo[2]);
     return SMX_OK;
 }
@@ -1149,7 +1190,9 @@ static int run_jackknife(const smx_nnls_problem *p, const TL *lib, const int32_t
     SMX_TRY_CUDA(cudaStreamSynchronize(s));
     if (hinfo[3] != 0) return set_error(SMX_ERR_ARGUMENT, "row_map holds an index outside [0, ld_lib)");
     if (hinfo[0] != 0) return set_error(SMX_ERR_NUMERIC, "Cholesky of rho' I + U U^T failed (info=%d)", hinfo[0]);
-    if (hinfo[1] != 0) return set_error(SMX_ERR_NUMERIC, "inverse of the Cholesky factor failed (info=%d)", hinfo[1]);
+    if (hinfo[1] != 0)
+        return set_error(SMX_ERR_NUMERIC, "inverse of rho' I + U U^T failed: a non-positive pivot of the FP32 seed or "
+                         "Newton-Schulz steps that do not converge");
     if (herr != 0) return set_error(SMX_ERR_CUDA, "split product kernel gave up waiting (code %d)", herr);
     return SMX_OK;
 }

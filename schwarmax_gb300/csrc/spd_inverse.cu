@@ -1,0 +1,235 @@
+// Inverse of a symmetric positive definite matrix in FP32 by blocked Gauss-Jordan
+// elimination without pivoting: the seed of the Newton-Schulz refinement of G^-1 in
+// the mixed NNLS (it replaces the float Cholesky inverse the reference's
+// jnp.linalg.cholesky step would suggest, nnls.py:121; only a residual well below 1
+// is needed, Newton-Schulz supplies the accuracy).
+//
+// For every 64-wide block k of the (padded) matrix, in place:
+//   P = A_kk^-1                       (one CTA, unblocked Gauss-Jordan in shared memory)
+//   R_k: = P A_k:                     (row panel, into a buffer)
+//   A_ij -= A_ik R_kj                 (i, j outside block k: 128 x 128 tiles, 8 x 8 per thread)
+//   A_ik = -A_ik P,  A_kj = R_kj,  A_kk = P
+// which leaves A^-1 after the last block.  2 m^3 flops on the FP32 pipe; the matrix
+// is padded to a multiple of 64 with an identity block.
+#include "smx_internal.cuh"
+
+namespace smx {
+
+constexpr int GJ_B = 64;      // elimination block
+constexpr int GJ_T = 128;     // update tile
+
+// unblocked Gauss-Jordan of the 64 x 64 diagonal block k (column-major, leading
+// dimension ld), P written column-major 64 x 64
+__global__ void __launch_bounds__(256) gj_diag_kernel(const float *__restrict__ A, int64_t ld, int64_t k0, float *P,
+                                                      int *flag) {
+    __shared__ float s[GJ_B][GJ_B + 1];   // s[row][col]
+    for (int e = threadIdx.x; e < GJ_B * GJ_B; e += blockDim.x) {
+        const int r = e % GJ_B, c = e / GJ_B;
+        s[r][c] = A[(k0 + r) + ld * (k0 + c)];
+    }
+    __syncthreads();
+    constexpr int PER = GJ_B * GJ_B / 256;
+    for (int k = 0; k < GJ_B; ++k) {
+        const float piv = s[k][k];
+        if (!(piv > 0.0f)) {
+            if (threadIdx.x == 0) atomicExch(flag, 1);
+            return;   // uniform: every thread read the same pivot
+        }
+        const float ip = 1.0f / piv;
+        float nv[PER];
+#pragma unroll
+        for (int q = 0; q < PER; ++q) {
+            const int e = threadIdx.x + q * 256;
+            const int r = e % GJ_B, c = e / GJ_B;
+            float v;
+            if (r == k) v = (c == k) ? ip : s[k][c] * ip;
+            else if (c == k) v = -s[r][k] * ip;
+            else v = s[r][c] - s[r][k] * (s[k][c] * ip);
+            nv[q] = v;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < PER; ++q) {
+            const int e = threadIdx.x + q * 256;
+            s[e % GJ_B][e / GJ_B] = nv[q];
+        }
+        __syncthreads();
+    }
+    for (int e = threadIdx.x; e < GJ_B * GJ_B; e += blockDim.x) P[e] = s[e % GJ_B][e / GJ_B];
+}
+
+// R (64 x mp, column-major ld 64) = P A[k block rows, :]; grid over 128-column tiles
+__global__ void __launch_bounds__(256) gj_row_kernel(const float *__restrict__ A, int64_t ld, int64_t k0,
+                                                     const float *__restrict__ P, float *R) {
+    __shared__ float sp[GJ_B][GJ_B + 1];
+    __shared__ float sa[GJ_B][GJ_T + 1];
+    const int64_t j0 = (int64_t)blockIdx.x * GJ_T;
+    for (int e = threadIdx.x; e < GJ_B * GJ_B; e += blockDim.x) sp[e % GJ_B][e / GJ_B] = P[e];
+    for (int e = threadIdx.x; e < GJ_B * GJ_T; e += blockDim.x) {
+        const int r = e % GJ_B, c = e / GJ_B;
+        sa[r][c] = A[(k0 + r) + ld * (j0 + c)];
+    }
+    __syncthreads();
+    // each thread: row r = tid % 64, columns c = tid / 64 + 4 q
+    const int r = threadIdx.x % GJ_B;
+    for (int c = threadIdx.x / GJ_B; c < GJ_T; c += 4) {
+        float acc = 0.f;
+#pragma unroll 16
+        for (int l = 0; l < GJ_B; ++l) acc += sp[r][l] * sa[l][c];
+        R[r + (int64_t)GJ_B * (j0 + c)] = acc;
+    }
+}
+
+// A_ij -= A_ik R_kj for the 128 x 128 tile (blockIdx.x, blockIdx.y), skipping the
+// rows and columns of block k; 8 x 8 outputs per thread
+__global__ void __launch_bounds__(256) gj_update_kernel(float *A, int64_t ld, int64_t k0, const float *__restrict__ R) {
+    __shared__ float sc[GJ_B][GJ_T + 4];   // sc[l][i]: A[i0 + i, k0 + l]
+    __shared__ float sr[GJ_B][GJ_T + 4];   // sr[l][j]: R[l, j0 + j]
+    const int64_t i0 = (int64_t)blockIdx.x * GJ_T, j0 = (int64_t)blockIdx.y * GJ_T;
+    const bool rows_hit = (k0 >= i0 && k0 < i0 + GJ_T), cols_hit = (k0 >= j0 && k0 < j0 + GJ_T);
+    if (rows_hit && cols_hit && GJ_T == 2 * GJ_B) {
+        // the tile holds the 64 x 64 diagonal block; its other three quarters are
+        // still updated below
+    }
+    for (int e = threadIdx.x; e < GJ_B * GJ_T; e += blockDim.x) {
+        const int i = e % GJ_T, l = e / GJ_T;
+        sc[l][i] = A[(i0 + i) + ld * (k0 + l)];
+        sr[l][i] = R[l + (int64_t)GJ_B * (j0 + i)];
+    }
+    __syncthreads();
+    const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;   // 16 x 16 threads, 8 x 8 each
+    float acc[8][8];
+#pragma unroll
+    for (int a = 0; a < 8; ++a)
+#pragma unroll
+        for (int b = 0; b < 8; ++b) acc[a][b] = 0.f;
+#pragma unroll 4
+    for (int l = 0; l < GJ_B; ++l) {
+        float ci[8], rj[8];
+#pragma unroll
+        for (int a = 0; a < 8; ++a) ci[a] = sc[l][tx + 16 * a];
+#pragma unroll
+        for (int b = 0; b < 8; ++b) rj[b] = sr[l][ty + 16 * b];
+#pragma unroll
+        for (int a = 0; a < 8; ++a)
+#pragma unroll
+            for (int b = 0; b < 8; ++b) acc[a][b] += ci[a] * rj[b];
+    }
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+        const int64_t j = j0 + ty + 16 * b;
+        if (j >= k0 && j < k0 + GJ_B) continue;
+#pragma unroll
+        for (int a = 0; a < 8; ++a) {
+            const int64_t i = i0 + tx + 16 * a;
+            if (i >= k0 && i < k0 + GJ_B) continue;
+            A[i + ld * j] -= acc[a][b];
+        }
+    }
+}
+
+// A_ik = -A_ik P for the rows of a 128-row tile outside block k; the tile that holds
+// block k also writes A_kk = P.  The row panel A_kj = R_kj is copied by gj_copy_kernel.
+__global__ void __launch_bounds__(256) gj_col_kernel(float *A, int64_t ld, int64_t k0, const float *__restrict__ P) {
+    __shared__ float sp[GJ_B][GJ_B + 1];
+    __shared__ float sa[GJ_T][GJ_B + 1];
+    const int64_t i0 = (int64_t)blockIdx.x * GJ_T;
+    for (int e = threadIdx.x; e < GJ_B * GJ_B; e += blockDim.x) sp[e % GJ_B][e / GJ_B] = P[e];
+    for (int e = threadIdx.x; e < GJ_T * GJ_B; e += blockDim.x) {
+        const int i = e % GJ_T, l = e / GJ_T;
+        sa[i][l] = A[(i0 + i) + ld * (k0 + l)];
+    }
+    __syncthreads();
+    const int i = threadIdx.x % GJ_T;
+    const int64_t gi = i0 + i;
+    const bool inblk = gi >= k0 && gi < k0 + GJ_B;
+    for (int c = threadIdx.x / GJ_T; c < GJ_B; c += 2) {
+        float v;
+        if (inblk) {
+            v = sp[gi - k0][c];
+        } else {
+            float acc = 0.f;
+#pragma unroll 16
+            for (int l = 0; l < GJ_B; ++l) acc += sa[i][l] * sp[l][c];
+            v = -acc;
+        }
+        A[gi + ld * (k0 + c)] = v;
+    }
+}
+
+__global__ void gj_copy_kernel(float *A, int64_t ld, int64_t k0, const float *__restrict__ R, int64_t mp) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < GJ_B * mp; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = e % GJ_B, j = e / GJ_B;
+        if (j >= k0 && j < k0 + GJ_B) continue;
+        A[(k0 + r) + ld * j] = R[e];
+    }
+}
+
+// padded copy: Ap (mp x mp) = G (m x m, double) in float, identity on the padding
+__global__ void gj_pad_kernel(const double *__restrict__ G, int64_t m, float *Ap, int64_t mp) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < mp * mp; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = e % mp, c = e / mp;
+        Ap[e] = (r < m && c < m) ? (float)G[r + m * c] : (r == c ? 1.0f : 0.0f);
+    }
+}
+
+int64_t spd_inverse_padded(int64_t m) { return (m + GJ_T - 1) / GJ_T * GJ_T; }
+
+size_t spd_inverse_workspace(int64_t m) {
+    const int64_t mp = spd_inverse_padded(m);
+    return (size_t)(mp * mp + GJ_B * GJ_B + GJ_B * mp) * sizeof(float) + 256;
+}
+
+// Ap (mp x mp float, padded by gj_pad_kernel) is overwritten by its inverse.
+// ws: GJ_B^2 + GJ_B mp floats of scratch plus an int flag (set when a pivot is not positive).
+int spd_inverse_inplace(float *Ap, int64_t mp, float *ws, int *flag, cudaStream_t s) {
+    float *P = ws, *R = ws + GJ_B * GJ_B;
+    const unsigned tiles = (unsigned)(mp / GJ_T);
+    for (int64_t k0 = 0; k0 < mp; k0 += GJ_B) {
+        gj_diag_kernel<<<1, 256, 0, s>>>(Ap, mp, k0, P, flag);
+        gj_row_kernel<<<tiles, 256, 0, s>>>(Ap, mp, k0, P, R);
+        gj_update_kernel<<<dim3(tiles, tiles), 256, 0, s>>>(Ap, mp, k0, R);
+        gj_col_kernel<<<tiles, 256, 0, s>>>(Ap, mp, k0, P);
+        gj_copy_kernel<<<(unsigned)((GJ_B * mp + 255) / 256), 256, 0, s>>>(Ap, mp, k0, R, mp);
+        count_launch(5);
+    }
+    SMX_TRY_CUDA(cudaGetLastError());
+    return SMX_OK;
+}
+
+}  // namespace smx
+
+using namespace smx;
+
+extern "C" int smx_spd_inverse_f32_workspace_size(int64_t m, size_t *bytes) {
+    if (m < 1 || !bytes) return set_error(SMX_ERR_ARGUMENT, "smx_spd_inverse_f32_workspace_size: bad argument");
+    const int64_t mp = spd_inverse_padded(m);
+    *bytes = (size_t)mp * mp * sizeof(float) + spd_inverse_workspace(m) + 256;
+    return SMX_OK;
+}
+
+extern "C" int smx_spd_inverse_f32(const double *G, int64_t m, float *Xinv, void *workspace, size_t workspace_bytes,
+                                   void *stream) {
+    if (m < 1 || m > 46340 || !G || !Xinv || !workspace)
+        return set_error(SMX_ERR_ARGUMENT, "smx_spd_inverse_f32: bad argument");
+    size_t need = 0;
+    int st = smx_spd_inverse_f32_workspace_size(m, &need);
+    if (st) return st;
+    if (workspace_bytes < need) return set_error(SMX_ERR_WORKSPACE, "smx_spd_inverse_f32: workspace too small");
+    cudaStream_t s = (cudaStream_t)stream;
+    const int64_t mp = spd_inverse_padded(m);
+    float *Ap = (float *)workspace;
+    float *ws = Ap + mp * mp;
+    int *flag = (int *)(ws + GJ_B * GJ_B + GJ_B * mp);
+    SMX_TRY_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), s));
+    gj_pad_kernel<<<4864, 256, 0, s>>>(G, m, Ap, mp);
+    count_launch();
+    if ((st = spd_inverse_inplace(Ap, mp, ws, flag, s))) return st;
+    SMX_TRY_CUDA(cudaMemcpy2DAsync(Xinv, m * sizeof(float), Ap, mp * sizeof(float), m * sizeof(float), m,
+                                   cudaMemcpyDeviceToDevice, s));
+    int hflag = 0;
+    SMX_TRY_CUDA(cudaMemcpyAsync(&hflag, flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+    SMX_TRY_CUDA(cudaStreamSynchronize(s));
+    if (hflag) return set_error(SMX_ERR_NUMERIC, "smx_spd_inverse_f32: a pivot was not positive");
+    return SMX_OK;
+}

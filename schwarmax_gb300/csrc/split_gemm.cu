@@ -129,6 +129,7 @@ struct GemmParams {
     float *R;
     int64_t ld;
     int *err;
+    const int *skip;   // optional: the kernel returns at once when *skip != 0
 };
 
 // output tile index -> (row tile, column tile)
@@ -177,6 +178,7 @@ __global__ void __launch_bounds__(320, 1) gemm_kernel(const GemmParams p) {
     uint32_t *tmem_holder = (uint32_t *)(mma_done + 1);
     volatile int *abort_flag = (volatile int *)(tmem_holder + 1);
 
+    if (p.skip && *p.skip) return;   // uniform over the grid, before any barrier or allocation
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t u0 = p.units * blockIdx.x / gridDim.x, u1 = p.units * (blockIdx.x + 1) / gridDim.x;
 
@@ -400,7 +402,8 @@ __global__ void __launch_bounds__(320, 1) gemm_kernel(const GemmParams p) {
 // max |x| per row, as the bits of a non-negative double (ordered like the values)
 template <typename T>
 __global__ void rowmax_kernel(const T *__restrict__ src, int64_t sr, int64_t sc, int64_t rows, int64_t k,
-                              unsigned long long *rowmax, int rows_fast, int skip_diag) {
+                              unsigned long long *rowmax, int rows_fast, int skip_diag, const int *skip) {
+    if (skip && *skip) return;
     if (rows_fast) {   // consecutive threads on consecutive rows; blocks along k
         const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
         if (r >= rows) return;
@@ -431,7 +434,9 @@ __device__ __forceinline__ int scale_exponent(double mx) {
     return e;
 }
 
-__global__ void expo_kernel(const unsigned long long *rowmax, int32_t *expo, int64_t rows, int64_t rows_padded) {
+__global__ void expo_kernel(const unsigned long long *rowmax, int32_t *expo, int64_t rows, int64_t rows_padded,
+                            const int *skip) {
+    if (skip && *skip) return;
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < rows_padded; r += (int64_t)gridDim.x * blockDim.x)
         expo[r] = r < rows ? scale_exponent(__longlong_as_double((long long)rowmax[r])) : 0;
 }
@@ -441,7 +446,8 @@ __global__ void expo_kernel(const unsigned long long *rowmax, int32_t *expo, int
 template <typename T, int S>
 __global__ void slice_rows_kernel(const T *__restrict__ src, int64_t sr, int64_t sc, int64_t rows, int64_t k,
                                   const int32_t *__restrict__ expo, __nv_bfloat16 *slices, int tile_rows,
-                                  int64_t k_tiles, int64_t slice_elems, int k_fast, int skip_diag) {
+                                  int64_t k_tiles, int64_t slice_elems, int k_fast, int skip_diag, const int *skip) {
+    if (skip && *skip) return;
     extern __shared__ __align__(16) unsigned char sm_raw[];
     __nv_bfloat16 *tile = (__nv_bfloat16 *)sm_raw;   // S x tile_rows x KT
     const int64_t kt = blockIdx.x, rt = blockIdx.y;
@@ -480,7 +486,8 @@ __global__ void slice_rows_kernel(const T *__restrict__ src, int64_t sr, int64_t
 // ------------------------------------------------------------------ host side
 
 template <int SA, int SB, int LMAX, int NT, int EXACT>
-static int launch_gemm(const Operand &A, const Operand &B, const Acc &acc, bool lower_only, int *err, cudaStream_t s) {
+static int launch_gemm(const Operand &A, const Operand &B, const Acc &acc, bool lower_only, int *err, cudaStream_t s,
+                       const int *skip) {
     // as many stages as fit in 227 KB of shared memory (2 or 3)
     constexpr int STAGES = Cfg<SA, SB, LMAX, NT, EXACT, 3>::SMEM <= 232448 ? 3 : 2;
     using C = Cfg<SA, SB, LMAX, NT, EXACT, STAGES>;
@@ -508,6 +515,7 @@ static int launch_gemm(const Operand &A, const Operand &B, const Acc &acc, bool 
     p.R = acc.R;
     p.ld = acc.ld;
     p.err = err;
+    p.skip = skip;
     int64_t grid = sms;
     if (grid > p.units) grid = p.units;
     gemm_kernel<SA, SB, LMAX, NT, EXACT, STAGES><<<(unsigned)grid, C::THREADS, C::SMEM, s>>>(p);
@@ -526,7 +534,8 @@ int exact_levels(const Operand &A, const Operand &B) {
 // 128 tensor-memory columns); 64-wide tiles for five (six accumulators), for
 // operands whose rows are dominated by one element (an inverse's diagonal);
 // 7 x 7 slices use pairs up to s + t = 8, four exact levels and 96-wide tiles.
-int gemm(const Operand &A, const Operand &B, const Acc &acc, bool lower_only, int *err, cudaStream_t s, int lmax) {
+int gemm(const Operand &A, const Operand &B, const Acc &acc, bool lower_only, int *err, cudaStream_t s, int lmax,
+         const int *skip) {
     if (!A.slices || !A.expo || !B.slices || !B.expo || !acc.T || !acc.R || !err)
         return set_error(SMX_ERR_ARGUMENT, "split gemm: operand or accumulator without storage");
     if (acc.ld < A.rows) return set_error(SMX_ERR_ARGUMENT, "split gemm: accumulator leading dimension too small");
@@ -535,26 +544,26 @@ int gemm(const Operand &A, const Operand &B, const Acc &acc, bool lower_only, in
     if (lower_only && B.tile_rows != MT) return set_error(SMX_ERR_ARGUMENT, "split gemm: lower_only needs square tiles");
     const int key = A.S * 10 + B.S;
     if (B.tile_rows == 112 && key == 45 && lmax == 7)
-        return launch_gemm<4, 5, 7, 112, 3>(A, B, acc, lower_only, err, s);
+        return launch_gemm<4, 5, 7, 112, 3>(A, B, acc, lower_only, err, s, skip);
     if (lmax != 0) return set_error(SMX_ERR_UNSUPPORTED, "split gemm: no kernel with pairs up to s + t = %d", lmax);
     if (B.tile_rows == 112) {
         switch (key) {
-            case 44: return launch_gemm<4, 4, 8, 112, 3>(A, B, acc, lower_only, err, s);
-            case 45: return launch_gemm<4, 5, 9, 112, 3>(A, B, acc, lower_only, err, s);
-            case 54: return launch_gemm<5, 4, 9, 112, 3>(A, B, acc, lower_only, err, s);
-            case 55: return launch_gemm<5, 5, 10, 112, 3>(A, B, acc, lower_only, err, s);
+            case 44: return launch_gemm<4, 4, 8, 112, 3>(A, B, acc, lower_only, err, s, skip);
+            case 45: return launch_gemm<4, 5, 9, 112, 3>(A, B, acc, lower_only, err, s, skip);
+            case 54: return launch_gemm<5, 4, 9, 112, 3>(A, B, acc, lower_only, err, s, skip);
+            case 55: return launch_gemm<5, 5, 10, 112, 3>(A, B, acc, lower_only, err, s, skip);
             default: break;
         }
     } else if (B.tile_rows == 128) {
         switch (key) {
-            case 44: return launch_gemm<4, 4, 8, 128, 3>(A, B, acc, lower_only, err, s);
-            case 55: return launch_gemm<5, 5, 10, 128, 3>(A, B, acc, lower_only, err, s);
+            case 44: return launch_gemm<4, 4, 8, 128, 3>(A, B, acc, lower_only, err, s, skip);
+            case 55: return launch_gemm<5, 5, 10, 128, 3>(A, B, acc, lower_only, err, s, skip);
             default: break;
         }
     } else if (B.tile_rows == 96) {
-        if (key == 77) return launch_gemm<7, 7, 8, 96, 4>(A, B, acc, lower_only, err, s);
+        if (key == 77) return launch_gemm<7, 7, 8, 96, 4>(A, B, acc, lower_only, err, s, skip);
     } else if (B.tile_rows == 64) {
-        if (key == 55) return launch_gemm<5, 5, 10, 64, 5>(A, B, acc, lower_only, err, s);
+        if (key == 55) return launch_gemm<5, 5, 10, 64, 5>(A, B, acc, lower_only, err, s, skip);
     }
     return set_error(SMX_ERR_UNSUPPORTED, "split gemm: no kernel for %d x %d slices with %d-row column tiles", A.S, B.S,
                      B.tile_rows);
@@ -568,7 +577,7 @@ static inline unsigned grid_for(int64_t count, int bs) {
 
 template <typename T>
 int slice_rows(const T *src, int64_t sr, int64_t sc, const Operand &op, unsigned long long *rowmax, cudaStream_t s,
-               bool skip_diag) {
+               bool skip_diag, const int *skip) {
     if (!src || !op.slices || !op.expo || !rowmax)
         return set_error(SMX_ERR_ARGUMENT, "slice_rows: operand without storage");
     const int64_t rows_padded = op.row_tiles * op.tile_rows;
@@ -577,13 +586,13 @@ int slice_rows(const T *src, int64_t sr, int64_t sc, const Operand &op, unsigned
     const bool rows_fast = sr == 1;
     if (rows_fast) {
         dim3 g((unsigned)((op.rows + 255) / 256), (unsigned)(op.k < 64 ? op.k : 64));
-        rowmax_kernel<T><<<g, 256, 0, s>>>(src, sr, sc, op.rows, op.k, rowmax, 1, skip_diag ? 1 : 0);
+        rowmax_kernel<T><<<g, 256, 0, s>>>(src, sr, sc, op.rows, op.k, rowmax, 1, skip_diag ? 1 : 0, skip);
     } else {
         rowmax_kernel<T><<<grid_for(op.rows * 32, 256), 256, 0, s>>>(src, sr, sc, op.rows, op.k, rowmax, 0,
-                                                                   skip_diag ? 1 : 0);
+                                                                   skip_diag ? 1 : 0, skip);
     }
     count_launch();
-    expo_kernel<<<grid_for(rows_padded, 256), 256, 0, s>>>(rowmax, op.expo, op.rows, rows_padded);
+    expo_kernel<<<grid_for(rows_padded, 256), 256, 0, s>>>(rowmax, op.expo, op.rows, rows_padded, skip);
     count_launch();
     dim3 g((unsigned)op.k_tiles, (unsigned)op.row_tiles);
     const size_t sm = (size_t)op.S * op.tile_rows * KT * sizeof(__nv_bfloat16);
@@ -594,7 +603,7 @@ int slice_rows(const T *src, int64_t sr, int64_t sc, const Operand &op, unsigned
         SMX_TRY_CUDA(cudaFuncSetAttribute(slice_rows_kernel<T, NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
                                           (int)sm));                                                             \
         slice_rows_kernel<T, NS><<<g, 256, sm, s>>>(src, sr, sc, op.rows, op.k, op.expo, op.slices, op.tile_rows,  \
-                                                    op.k_tiles, op.slice_elems(), k_fast, skip_diag ? 1 : 0);    \
+                                                    op.k_tiles, op.slice_elems(), k_fast, skip_diag ? 1 : 0, skip); \
         break;
         SMX_SLICE_CASE(4)
         SMX_SLICE_CASE(5)
@@ -608,9 +617,9 @@ int slice_rows(const T *src, int64_t sr, int64_t sc, const Operand &op, unsigned
 }
 
 template int slice_rows<float>(const float *, int64_t, int64_t, const Operand &, unsigned long long *, cudaStream_t,
-                               bool);
+                               bool, const int *);
 template int slice_rows<double>(const double *, int64_t, int64_t, const Operand &, unsigned long long *, cudaStream_t,
-                                bool);
+                                bool, const int *);
 
 }  // namespace split
 }  // namespace smx

@@ -138,8 +138,10 @@ int exact_levels(const Operand &A, const Operand &B);
 // in the kernel gave up.
 // lmax = 0 forms every slice pair; lmax = 7 (4 x 5 slices, 112-wide tiles) drops
 // the pairs s + t >= 8, about 2^-47 of max|A| max|B| per product term.
+// skip (optional device flag): when *skip != 0 at run time the launched kernels
+// return at once (a step of an iteration that has converged on the device).
 int gemm(const Operand &A, const Operand &B, const Acc &acc, bool lower_only, int *err, cudaStream_t s,
-         int lmax = 0);
+         int lmax = 0, const int *skip = nullptr);
 
 // Row scales and slices of a strided matrix: element (r, c) at src[r*sr + c*sc],
 // r < rows, c < k.  Src is float or double.  expo and slices of op must be allocated;
@@ -147,7 +149,7 @@ int gemm(const Operand &A, const Operand &B, const Acc &acc, bool lower_only, in
 // entries r == c are taken as 0 (the off-diagonal part of a square matrix).
 template <typename T>
 int slice_rows(const T *src, int64_t sr, int64_t sc, const Operand &op, unsigned long long *rowmax,
-               cudaStream_t s, bool skip_diag = false);
+               cudaStream_t s, bool skip_diag = false, const int *skip = nullptr);
 
 }  // namespace split
 }  // namespace smx

@@ -124,3 +124,19 @@ def test_split_gemm_nonnegative_library_shape(K):
     _check(K.split_gemm(U, D), U, D, 31)
     Ut = U.t().contiguous()
     _check(K.split_gemm(U, Ut), U, Ut, 31)
+
+
+@pytest.mark.parametrize("m", [5, 200, 777])
+def test_spd_inverse_seed(m):
+    """The FP32 blocked Gauss-Jordan inverse that seeds Newton-Schulz: residual
+    ||I - G X||_F far below 1 for a matrix with the NNLS's structure (c I + U U^T)."""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from schwarmax_gb300 import kernels
+    g = torch.Generator(device="cuda").manual_seed(m)
+    U = torch.randn(m, 2 * m + 3, generator=g, device="cuda", dtype=torch.float64)
+    U = U * torch.logspace(0, 2, m, device="cuda", dtype=torch.float64)[:, None]    # uneven row scales
+    G = (U @ U.t() + (U * U).sum() / U.shape[1] * torch.eye(m, device="cuda", dtype=torch.float64)).contiguous()
+    X = kernels.spd_inverse_f32(G).double()
+    R = torch.eye(m, device="cuda", dtype=torch.float64) - G @ X
+    assert float(torch.linalg.norm(R)) < 1e-2
