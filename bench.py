@@ -131,6 +131,7 @@ def run_ours(args, rank, world, local):
     dict_data, theta = synthetic.make_dataset(cfg, seed=args.seed)
     setup_s = time.time() - t0
     st = cfg.settings("mixed")
+    st.autotune = bool(getattr(args, "autotune", False))
     dd = engine.DeviceData(dict_data, n_real=st.n_real)
     nb = cfg.n_bins
     nc = cfg.n_grid[0] * cfg.n_grid[1] * cfg.n_grid[2]
@@ -143,9 +144,9 @@ def run_ours(args, rank, world, local):
         if batched:
             th = points.copy()
             th[:, 10] = th[:, 10] + 0.002 * ((i % 5) - 2)
-            logl, r = log_likelihoods_batch(th, dd, nb, nc, **kw)
+            logl, r = log_likelihoods_batch(th, dd, nb, nc, keep=args.jackknife, **kw)
             if args.jackknife:
-                r["jackknife"] = jackknife_batch(th, dd, nb, nc, st, cfg.admm_iters)
+                r["jackknife"] = jackknife_batch(th, r, dd, nb, st, cfg.admm_iters)
             m = torch.max(logl, dim=1, keepdim=True).values
             return m[:, 0] + torch.log(torch.mean(torch.exp(logl - m), dim=1)), r
         th = theta.copy()
@@ -282,22 +283,37 @@ def run_ours(args, rank, world, local):
         torch.distributed.destroy_process_group()
 
 
-def jackknife_batch(thetas, dd, nb, nc, st, maxiter):
-    """calculate_delta_chi2 (leave-one-bin-out jackknife) at every point of a batch."""
-    from schwarmax_gb300.likelihood import calculate_delta_chi2
-    return [calculate_delta_chi2(th, dd, nb, nc, settings=st, nnls_maxiter=maxiter) for th in thetas]
+def jackknife_batch(thetas, r, dd, nb, st, maxiter):
+    """calculate_delta_chi2 (leave-one-bin-out jackknife, one replicate per bin) at every
+    point of a batch, on the libraries the batch built: each point's replicates run as
+    one batched mixed-precision solve."""
+    from schwarmax_gb300.likelihood import chi2_func, grid_of, unpack_params
+    from schwarmax_gb300.model import jackknife_of_library
+    from schwarmax_gb300.potentials import potential_struct
+    grid = grid_of(dd)
+    libs = [lib for chunk in r["libraries"] for lib in chunk]
+    out = []
+    for th, lib in zip(thetas, libs):
+        halo, bary = unpack_params(th)
+        pot = potential_struct(bary, halo, st.bulge_mass)
+        out.append(float(jackknife_of_library(chi2_func, lib, pot, bary, dd, grid, st, maxiter, 1.0, nb)))
+    return out
 
 
 def precision_and_fp64(cfg, dd, grid, nb, theta, st, step, mixed_evals_per_s):
-    """Delta chi^2 of the mixed solver against the FP64 solver on one library, and the
-    plain-FP64 evaluation rate.  The FP64 orbit integration of the full workload
-    takes about an hour on this part (FP64 is 1/64 of the FP32 rate), so its time is
-    measured on all orbits over 1/50 of the horizon and scaled by the attempt count;
-    every other FP64 stage is timed at full size."""
+    """Errors of the mixed evaluation against plain FP64, and the plain-FP64 rate.
+
+    * same library: the mixed NNLS + maps against the FP64 NNLS + maps on the float
+      library of the mixed run (the solver's contract, Delta chi^2 <= 0.1);
+    * the full FP64 evaluation (FP64 ICs, orbits, binning, target, NNLS, maps), timed
+      stage by stage with CUDA events; against it: the end-to-end Delta chi^2, the
+      orbits' end states, their Jacobi-integral drift, and the per-bin moments of the
+      two libraries under the same (FP64) weights;
+    * bin indices: the FP32 kernel's (R, z, phi) cells and sky pixels of every stored
+      sample image against the same float operations with a correctly rounded atan2."""
     import torch
 
     from schwarmax_gb300 import _lib, engine, kernels
-    from schwarmax_gb300._lib import SMX_MODE_SAMPLED, SmxIntegrator
     from schwarmax_gb300.likelihood import log_mean_exp, unpack_params
     from schwarmax_gb300.potentials import potential_struct
 
@@ -307,18 +323,14 @@ def precision_and_fp64(cfg, dd, grid, nb, theta, st, step, mixed_evals_per_s):
     lib64 = lib32.double()
     d = r_m["data"]
     n = lib64.shape[0]
-    row_scale, Y = engine.nnls_inputs(d, dd, grid.n_cells, (math.sqrt(5.0), math.sqrt(5.0), 1.0))
+    nc = grid.n_cells
+    row_scale, Y = engine.nnls_inputs(d, dd, nc, (math.sqrt(5.0), math.sqrt(5.0), 1.0))
     w_init = float((d["y_rz"].sum() / n).item())
-    torch.cuda.synchronize()
-    t0 = time.time()
-    W64 = kernels.nnls_admm(lib64, engine.row_map(grid.n_cells, nb), row_scale, Y, cfg.admm_iters, 1.0, w_init,
-                            mixed=False)
+    W64 = kernels.nnls_admm(lib64, engine.row_map(nc, nb), row_scale, Y, cfg.admm_iters, 1.0, w_init, mixed=False)
     y_xy_b, y_h_b, sh = engine.likelihood_data(dd)
     lum = float(d["mmpo"].item()) * d["l2m"]
-    _, logl_64 = kernels.model_maps(lib64, grid.n_cells, nb, W64, d["gamma"].contiguous(), dd.v0, dd.s,
+    _, logl_64 = kernels.model_maps(lib64, nc, nb, W64, d["gamma"].contiguous(), dd.v0, dd.s,
                                     d["y_rz"].contiguous(), dd.xy, y_xy_b, y_h_b, sh, lum, 1.0, want_maps=False)
-    torch.cuda.synchronize()
-    t_nnls64 = time.time() - t0
     dchi2 = (2 * (logl_m - logl_64)).abs()
     wm = r_m["W"]
     out = {"precision_ok": bool(float(dchi2.max().item()) <= 0.1),
@@ -327,53 +339,112 @@ def precision_and_fp64(cfg, dd, grid, nb, theta, st, step, mixed_evals_per_s):
            "dchi2_marginal_same_library": abs(2 * float((log_mean_exp(logl_m) - log_mean_exp(logl_64)).item())),
            "chi2_scale": float((-2 * logl_64).median().item()),
            "weights_max_rel_same_library": float(((wm - W64).abs().max() / W64.abs().max()).item())}
-    # plain FP64 stage times
+    # ---- the plain FP64 evaluation, every stage at full size
     halo, bary = unpack_params(theta)
     st64 = engine.Settings(**{**st.__dict__, "precision": "fp64"})
     pot = potential_struct(bary, halo, st64.bulge_mass)
-    pos, nrm, uni = dd.cast(torch.float64, st64.n_real)
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
-    ev[0].record()
-    ic = kernels.initial_conditions(pot, pos, nrm, uni, st64.n_real, st64.n_periods, st64.steps_per_period)
-    ev[1].record()
-    frac = 1.0 / 50.0
-    ns = max(1, int(round(st64.n_samples * frac)))
-    bufs = kernels.IntegratorBuffers(ic["w0"].shape[1], ns, torch.float64, torch.device("cuda"))
-    icfg = SmxIntegrator(mode=SMX_MODE_SAMPLED, store_all=0, n_attempts=st64.n_attempts, n_samples=ns,
-                         max_attempts=st64.max_attempts, atol=st64.atol, rtol=st64.rtol, dt_min=st64.dt_min,
-                         dt_max=st64.dt_max, omega=-float(bary["Omega_bar"]))
-    ev[2].record()
-    kernels.integrate(pot, icfg, ic["w0"], ic["dt_init"], (ic["t_total"] * frac).contiguous(), bufs)
-    ev[3].record()
-    y_rz = kernels.density_target(pot, torch.float64, dd.R_grid, dd.z_grid, dd.phi_grid, dd.dR, dd.dz, dd.dphi,
-                                  dd.sample)
-    ev[4].record()
-    torch.cuda.synchronize()
-    att_short = float(bufs.info[_lib.INFO_NATT].sum().item())
-    att_full = float(r_m["lib"]["bufs"].info[_lib.INFO_NATT].double().sum().item())
-    t_ic = ev[0].elapsed_time(ev[1]) / 1e3
-    t_int = ev[2].elapsed_time(ev[3]) / 1e3 * att_full / max(att_short, 1.0)
-    t_tgt = ev[3].elapsed_time(ev[4]) / 1e3
-    # binning in FP64 at full size, on the mixed run's samples promoted to double
-    b32 = r_m["lib"]["bufs"]
-    b64 = kernels.IntegratorBuffers(b32.n_orb, b32.slots, torch.float64, torch.device("cuda"))
-    b64.samples.copy_(b32.samples)
-    b64.n_stored.copy_(b32.n_stored)
-    b64.info.copy_(b32.info)
-    geo = r_m["lib"]["geo"]
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    kernels.project_bin(geo, b64, r_m["lib"]["ic"]["t_total"].double(), dd.bin_mapping, dd.num_per_bin, dd.v0, dd.s)
-    e1.record()
-    torch.cuda.synchronize()
-    t_bin = e0.elapsed_time(e1) / 1e3
-    total64 = t_ic + t_int + t_tgt + t_bin + t_nnls64
+    holder = {}
+
+    def run64():
+        holder["r"] = engine.evaluate(pot, bary, dd, grid, st64, cfg.admm_iters, 1.0, want_maps=True)
+
+    stages64 = stage_breakdown(run64)
+    r64 = holder["r"]
+    total64 = stages64["total"] / 1e3
     out.update({"fp64_evals_per_s": 1.0 / total64, "mixed_over_fp64": mixed_evals_per_s * total64,
-                "fp64_stage_s": {"initial_conditions": t_ic, "integrate_scaled": t_int, "density_target": t_tgt,
-                                 "project_bin": t_bin, "nnls_and_maps": t_nnls64},
-                "fp64_integrator_sample": f"all {b32.n_orb} orbits over 1/50 of the horizon "
-                                          f"({att_short:.3g} attempts), scaled to {att_full:.3g} attempts"})
+                "fp64_stage_ms": stages64})
+    out["dchi2_end_to_end_vs_fp64"] = {"max": float((2 * (logl_m - r64["logl"])).abs().max()),
+                                       "median": float((2 * (logl_m - r64["logl"])).abs().median())}
+    # ---- orbit end states and Jacobi drift (FP32 vs FP64 orbits from the same draws)
+    b32, b64 = r_m["lib"]["bufs"], r64["lib"]["bufs"]
+    last32 = b32.samples[:6, torch.arange(b32.n_orb, device="cuda"), (b32.n_stored.long() - 1).clamp(min=0)].double()
+    last64 = b64.samples[:6, torch.arange(b64.n_orb, device="cuda"), (b64.n_stored.long() - 1).clamp(min=0)]
+    pos_err = (last32[:3] - last64[:3]).norm(dim=0) / last64[:3].norm(dim=0).clamp(min=1e-30)
+    q = torch.tensor([0.5, 0.9, 0.99], dtype=torch.float64, device="cuda")
+
+    def quant(x):
+        v = torch.quantile(x[torch.isfinite(x)][:1_000_000], q)
+        return {"median": float(v[0]), "p90": float(v[1]), "p99": float(v[2]), "max": float(x[torch.isfinite(x)].max())}
+
+    drift32 = (b32.info[_lib.INFO_EJ].double() / b32.info[_lib.INFO_EJ0].double() - 1).abs()
+    drift64 = (b64.info[_lib.INFO_EJ] / b64.info[_lib.INFO_EJ0] - 1).abs()
+    out["orbit_end_state_rel_error"] = quant(pos_err)
+    out["jacobi_drift_fp32"] = quant(drift32)
+    out["jacobi_drift_fp64"] = quant(drift64)
+    # ---- per-bin moments of the two libraries under the FP64 weights
+    W = r64["W"]
+    m32, _ = kernels.model_maps(lib64, nc, nb, W, r64["data"]["gamma"].contiguous(), dd.v0, dd.s,
+                                r64["data"]["y_rz"].contiguous(), dd.xy, y_xy_b, y_h_b, sh, lum, 1.0)
+    m64 = r64["maps"]
+    mp32, mp64 = engine.split_maps(m32, nc, nb), engine.split_maps(m64, nc, nb)
+    sd_rel = ((mp32["surface_density"] - mp64["surface_density"]).abs() / mp64["surface_density"].abs().clamp(min=1e-300))
+    mom = {"surface_density_rel": {"median": float(sd_rel.median()), "max": float(sd_rel.max())}}
+    for k in range(1, 5):
+        dh = (mp32[f"h{k}"] - mp64[f"h{k}"]).abs()
+        mom[f"h{k}_abs"] = {"median": float(dh.median()), "max": float(dh.max())}
+    out["per_bin_moments_fp32_vs_fp64_orbits"] = mom
+    # ---- bin indices of every stored sample image (FP32 kernel vs float ops with a correctly rounded atan2)
+    out["cell_index_check"] = index_check(r_m["lib"]["geo"], b32, dd)
     return out
+
+
+def index_check(geo, bufs, dd, max_samples=20_000_000):
+    """Counts the sample images whose Rzphi cell or sky pixel from the FP32 kernel
+    differs from the same IEEE float operations (utils.py:10-42, integrates.py:120-146)
+    evaluated with torch, where atan2 is the correctly rounded double atan2 rounded to
+    float.  Only atan2 may differ (CUDA's atan2f is not correctly rounded)."""
+    import torch
+
+    from schwarmax_gb300 import kernels
+    slots = bufs.slots
+    valid = torch.arange(slots, device="cuda")[None] < bufs.n_stored[:, None].long()     # (n_orb, slots)
+    pts = bufs.samples[:6].reshape(6, -1)[:, valid.reshape(-1)][:, :max_samples].contiguous()
+    N = pts.shape[1]
+    cells, bins, _ = kernels.sample_cells(geo, pts, dd.bin_mapping)
+    f = torch.float32
+    lo = [geo.R_lo, geo.z_lo, geo.phi_lo]
+    hi = [geo.R_hi, geo.z_hi, geo.phi_hi]
+    nn = [geo.nR, geo.nz, geo.nphi]
+    rot = torch.tensor(list(geo.rot), dtype=f, device="cuda")
+    n_cells = geo.nR * geo.nz * geo.nphi
+    bad_cell = 0
+    bad_pix = 0
+    for im in range(4 if geo.symmetry else 1):
+        sxy = -1.0 if im >= 2 else 1.0
+        sz = -1.0 if im in (1, 3) else 1.0
+        x, y, z = pts[0] * sxy, pts[1] * sxy, pts[2] * sz
+        R = torch.sqrt(x * x + y * y)
+        ph = torch.atan2(y.double(), x.double()).to(f)
+        flat = torch.zeros(N, dtype=torch.int64, device="cuda")
+        out_ = torch.zeros(N, dtype=torch.bool, device="cuda")
+        stride = 1
+        for v, a, b, m in zip((R, z, ph), lo, hi, nn):
+            span = torch.tensor(b, dtype=f) - torch.tensor(a, dtype=f)
+            norm = (v - torch.tensor(a, dtype=f, device="cuda")) / span.to("cuda")
+            out_ |= ~(norm < 1) | (norm < 0)
+            k = torch.floor(norm * float(m)).clamp(0, m - 1).long()
+            flat += k * stride
+            stride *= m
+        ref_cell = torch.where(out_, torch.full_like(flat, n_cells), flat)
+        bad_cell += int((ref_cell != cells[im].long()).sum())
+        X = (rot[0] * x + rot[1] * y) + rot[2] * z
+        Yv = (rot[3] * x + rot[4] * y) + rot[5] * z
+        pix = torch.zeros(N, dtype=torch.int64, device="cuda")
+        outp = torch.zeros(N, dtype=torch.bool, device="cuda")
+        stride = 1
+        for v, a, b, m in zip((X, Yv), (geo.X_lo, geo.Y_lo), (geo.X_hi, geo.Y_hi), (geo.nX, geo.nY)):
+            span = torch.tensor(b, dtype=f) - torch.tensor(a, dtype=f)
+            norm = (v - torch.tensor(a, dtype=f, device="cuda")) / span.to("cuda")
+            outp |= ~(norm < 1) | (norm < 0)
+            k = torch.floor(norm * float(m)).clamp(0, m - 1).long()
+            pix += k * stride
+            stride *= m
+        pix = torch.where(outp, torch.full_like(pix, geo.nX * geo.nY), pix)
+        ref_bin = dd.bin_mapping.long()[pix]
+        bad_pix += int((ref_bin != bins[im].long()).sum())
+    images = N * (4 if geo.symmetry else 1)
+    return {"images": images, "cell_mismatches": bad_cell, "aperture_mismatches": bad_pix,
+            "cell_mismatch_fraction": bad_cell / max(images, 1)}
 
 
 def stage_breakdown(fn):
@@ -579,6 +650,8 @@ def main():
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--points", type=int, default=64, help="parameter points per batch (--config 2)")
+    ap.add_argument("--autotune", action="store_true",
+                    help="--config 2: tuned integrator launch (blocks per SM, queue order; cached)")
     ap.add_argument("--jackknife", action="store_true",
                     help="--config 2: add the 400 leave-one-bin-out jackknife NNLS solves of every point")
     ap.add_argument("--adjoint", action="store_true",

@@ -44,16 +44,25 @@ typedef enum {
 
 typedef enum { SMX_FP32 = 0, SMX_FP64 = 1 } smx_precision;
 
-/* Canonical potential Phi = NFW + Miyamoto-Nagai + Dehnen-Aly T (bar) +
- * Dehnen-Aly V (bulge), all centred at the origin with symmetry axis +z.
- * Replaces potential_func / density_func of likelihood.py:13-71 (built from
- * potentials.py:18-65 and dehnen_bar.py:1318-1543).  The bar is a T3 model and
- * the bulge a V4 model; gamma is the needle slope (dehnen_bar.py:211-241). */
+/* Dehnen & Aly (2022) needle models of the bar and bulge slots
+ * (_make_explicit_fns, dehnen_bar.py:1272-1555): T1..T4 and V1..V4.  0 selects the
+ * slot's canonical model (bar T3, bulge V4).  T0 and V0 are not built. */
+enum { SMX_DEHNEN_DEFAULT = 0, SMX_DEHNEN_T1 = 1, SMX_DEHNEN_T2 = 2, SMX_DEHNEN_T3 = 3, SMX_DEHNEN_T4 = 4,
+       SMX_DEHNEN_V1 = 11, SMX_DEHNEN_V2 = 12, SMX_DEHNEN_V3 = 13, SMX_DEHNEN_V4 = 14 };
+
+/* Potential Phi = NFW + Miyamoto-Nagai + Dehnen-Aly bar + Dehnen-Aly bulge, all
+ * centred at the origin with symmetry axis +z.  With the default model types it is
+ * the canonical potential_func / density_func of likelihood.py:13-71 (built from
+ * potentials.py:18-65 and dehnen_bar.py:1318-1543): a T3 bar and a V4 bulge; gamma
+ * is the needle slope (dehnen_bar.py:211-241).  bar_type / bulge_type choose another
+ * member of the family for either slot (SMX_DEHNEN_*), for the forces, the
+ * integrator, the initial conditions and the density target alike. */
 typedef struct {
     double halo_M, halo_Rs, halo_qa, halo_qb, halo_qc;      /* NFW: M = 10**logM */
     double disc_M, disc_a, disc_b;                            /* MN: M, Rs_disc, Hs_disc */
-    double bar_M, bar_a, bar_b, bar_L, bar_gamma;             /* T3 */
-    double bulge_M, bulge_a, bulge_b, bulge_L, bulge_gamma;   /* V4 */
+    double bar_M, bar_a, bar_b, bar_L, bar_gamma;             /* T3 by default */
+    double bulge_M, bulge_a, bulge_b, bulge_L, bulge_gamma;   /* V4 by default */
+    int bar_type, bulge_type;                                 /* SMX_DEHNEN_* (0: default) */
 } smx_potential;
 
 /* One parameter point of a batched call: its potential and the frame's angular

@@ -161,6 +161,129 @@ def v4_rho(x, y, z, M, a, b, L, gamma):
     return (b * b * iz ** 3) * (0.375 * b * b / math.pi) * rh
 
 
+def t1_phi(x, y, z, M, a, b, L, gamma):
+    """dehnen_bar.py:1303-1307."""
+    Z = D.sqrt(z * z + b * b) + a
+    return -G * _needle(M, x, y, Z, L, gamma, (1,))[1]
+
+
+def t2_phi(x, y, z, M, a, b, L, gamma):
+    """dehnen_bar.py:1309-1316."""
+    Z = D.sqrt(z * z + b * b) + a
+    F = _needle(M, x, y, Z, L, gamma, (1, 3))
+    return -G * (F[1] + a * Z * F[3])
+
+
+def t4_phi(x, y, z, M, a, b, L, gamma):
+    """dehnen_bar.py:1328-1337."""
+    Z = D.sqrt(z * z + b * b) + a
+    aZ = a * Z
+    F = _needle(M, x, y, Z, L, gamma, (1, 3, 5, 7))
+    ph = F[1] + a * (Z - 0.4 * a) * F[3] + 0.6 * a * aZ * (Z + Z - a) * F[5] + aZ ** 3 * F[7]
+    return -G * ph
+
+
+def v1_phi(x, y, z, M, a, b, L, gamma):
+    """dehnen_bar.py:1339-1346."""
+    ze = D.sqrt(z * z + b * b)
+    Z = ze + a
+    hB2 = 0.5 * b * b
+    F = _needle(M, x, y, Z, L, gamma, (1, 3))
+    return -G * (F[1] + (hB2 * Z / ze) * F[3])
+
+
+def v2_phi(x, y, z, M, a, b, L, gamma):
+    """dehnen_bar.py:1348-1357."""
+    ze = D.sqrt(z * z + b * b)
+    Z = ze + a
+    aZ = a * Z
+    hB2 = 0.5 * b * b
+    F = _needle(M, x, y, Z, L, gamma, (1, 3, 5))
+    return -G * (F[1] + (aZ + hB2) * F[3] + (3 * hB2 * aZ * Z / ze) * F[5])
+
+
+def v3_phi(x, y, z, M, a, b, L, gamma):
+    """dehnen_bar.py:1359-1369."""
+    ze = D.sqrt(z * z + b * b)
+    Z = ze + a
+    aZ = a * Z
+    hB2 = 0.5 * b * b
+    F = _needle(M, x, y, Z, L, gamma, (1, 3, 5, 7))
+    ph = F[1] + (a * (Z - a / 3) + hB2) * F[3] + aZ * (aZ + 3 * hB2) * F[5] + (5 * hB2 * aZ ** 2 * Z / ze) * F[7]
+    return -G * ph
+
+
+def t1_rho(x, y, z, M, a, b, L, gamma):
+    """dehnen_bar.py:1399-1409."""
+    ze = D.sqrt(z * z + b * b)
+    iz = 1.0 / ze
+    Z = ze + a
+    F = _needle(M, x, y, Z, L, gamma, (3, 5))
+    return (b * b * iz ** 3) * (0.25 / math.pi) * (a * F[3] + 3 * Z * Z * ze * F[5])
+
+
+def t2_rho(x, y, z, M, a, b, L, gamma):
+    """dehnen_bar.py:1411-1423."""
+    ze = D.sqrt(z * z + b * b)
+    iz = 1.0 / ze
+    Z = ze + a
+    F = _needle(M, x, y, Z, L, gamma, (5, 7))
+    rh = (a * a * a + ze ** 3) * F[5] + 5 * a * Z * Z * Z * ze * F[7]
+    return (b * b * iz ** 3) * (0.75 / math.pi) * rh
+
+
+def t4_rho(x, y, z, M, a, b, L, gamma):
+    """dehnen_bar.py:1440-1456."""
+    ze = D.sqrt(z * z + b * b)
+    iz = 1.0 / ze
+    Z = ze + a
+    Z2, A2, AZ = Z * Z, a * a, a * Z
+    F = _needle(M, x, y, Z, L, gamma, (5, 7, 9, 11))
+    rh = (3 * F[5] + 15 * AZ * F[7]) * ze ** 3
+    rh = rh + 7 * A2 * Z * Z2 * ((6 * ze - 3 * a) * ze + A2) * F[9]
+    rh = rh + 63 * A2 * AZ * Z2 * Z2 * ze * F[11]
+    return (b * b * iz ** 3) * (0.25 / math.pi) * rh
+
+
+def v1_rho(x, y, z, M, a, b, L, gamma):
+    """dehnen_bar.py:1480-1493."""
+    ze = D.sqrt(z * z + b * b)
+    iz = 1.0 / ze
+    Z = ze + a
+    F = _needle(M, x, y, Z, L, gamma, (3, 5, 7))
+    rh = a * iz * iz * F[3] + 3 * a * Z * iz * F[5] + 5 * Z * Z * Z * F[7]
+    return (b * b * iz ** 3) * (0.375 * b * b / math.pi) * rh
+
+
+def v2_rho(x, y, z, M, a, b, L, gamma):
+    """dehnen_bar.py:1495-1508."""
+    ze = D.sqrt(z * z + b * b)
+    iz = 1.0 / ze
+    Z = ze + a
+    Z2, A2 = Z * Z, a * a
+    F = _needle(M, x, y, Z, L, gamma, (5, 7, 9))
+    rh = 3 * a * A2 * iz * iz * F[5] + 5 * Z2 * (ze * ze - 2 * a * ze + 3 * A2) * iz * F[7] + 35 * a * Z2 * Z2 * F[9]
+    return (b * b * iz ** 3) * (0.375 * b * b / math.pi) * rh
+
+
+def v3_rho(x, y, z, M, a, b, L, gamma):
+    """dehnen_bar.py:1510-1524."""
+    ze = D.sqrt(z * z + b * b)
+    iz = 1.0 / ze
+    Z = ze + a
+    Z2, A2, AZ = Z * Z, a * a, a * Z
+    F = _needle(M, x, y, Z, L, gamma, (7, 9, 11))
+    rh = 3 * ze ** 3 * (1 + (a * iz) ** 5) * F[7]
+    rh = rh + 7 * AZ * Z2 * iz * ((3 * ze - 4 * a) * ze + 3 * A2) * F[9]
+    rh = rh + 63 * A2 * Z * Z2 * Z2 * F[11]
+    return (b * b * iz ** 3) * (0.625 * b * b / math.pi) * rh
+
+
+DEHNEN_PHI = {1: t1_phi, 2: t2_phi, 3: t3_phi, 4: t4_phi, 11: v1_phi, 12: v2_phi, 13: v3_phi, 14: v4_phi}
+DEHNEN_RHO = {1: t1_rho, 2: t2_rho, 3: t3_rho, 4: t4_rho, 11: v1_rho, 12: v2_rho, 13: v3_rho, 14: v4_rho}
+DEHNEN_CODES = {"T1": 1, "T2": 2, "T3": 3, "T4": 4, "V1": 11, "V2": 12, "V3": 13, "V4": 14}
+
+
 # --------------------------------------------------------------------------
 # NFW and Miyamoto-Nagai
 # --------------------------------------------------------------------------
@@ -196,16 +319,20 @@ def phi(x, y, z, P):
     """potential_func (likelihood.py:46-71)."""
     p = nfw_phi(x, y, z, P["halo_M"], P["halo_Rs"], P["halo_qa"], P["halo_qb"], P["halo_qc"])
     p = p + mn_phi(x, y, z, P["disc_M"], P["disc_a"], P["disc_b"])
-    p = p + t3_phi(x, y, z, P["bar_M"], P["bar_a"], P["bar_b"], P["bar_L"], P["bar_gamma"])
-    p = p + v4_phi(x, y, z, P["bulge_M"], P["bulge_a"], P["bulge_b"], P["bulge_L"], P["bulge_gamma"])
+    fb = DEHNEN_PHI[P.get("bar_type", 3) or 3]
+    fu = DEHNEN_PHI[P.get("bulge_type", 14) or 14]
+    p = p + fb(x, y, z, P["bar_M"], P["bar_a"], P["bar_b"], P["bar_L"], P["bar_gamma"])
+    p = p + fu(x, y, z, P["bulge_M"], P["bulge_a"], P["bulge_b"], P["bulge_L"], P["bulge_gamma"])
     return p
 
 
 def rho(x, y, z, P):
     """density_func (likelihood.py:13-43)."""
     r = mn_rho(x, y, z, P["disc_M"], P["disc_a"], P["disc_b"])
-    r = r + t3_rho(x, y, z, P["bar_M"], P["bar_a"], P["bar_b"], P["bar_L"], P["bar_gamma"])
-    r = r + v4_rho(x, y, z, P["bulge_M"], P["bulge_a"], P["bulge_b"], P["bulge_L"], P["bulge_gamma"])
+    fb = DEHNEN_RHO[P.get("bar_type", 3) or 3]
+    fu = DEHNEN_RHO[P.get("bulge_type", 14) or 14]
+    r = r + fb(x, y, z, P["bar_M"], P["bar_a"], P["bar_b"], P["bar_L"], P["bar_gamma"])
+    r = r + fu(x, y, z, P["bulge_M"], P["bulge_a"], P["bulge_b"], P["bulge_L"], P["bulge_gamma"])
     return r
 
 

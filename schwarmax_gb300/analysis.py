@@ -102,7 +102,7 @@ def build_Lcirc_of_E(potential_fn, potential_args=(), R_min=1e-2, R_max=1e2, n_g
     tensors (returns device tensors)."""
     require_canonical(None, potential_fn)
     params_baryon, params_halo = potential_args
-    pot = potential_struct(params_baryon, params_halo, bulge_mass)
+    pot = potential_struct(params_baryon, params_halo, bulge_mass, **potential_fn.types)
     E = torch.empty(int(n_grid), dtype=torch.float64, device="cuda")
     L = torch.empty_like(E)
     call("smx_lcirc_table", ctypes.byref(pot), float(R_min), float(R_max), int(n_grid), float(dR), _ptr(E), _ptr(L),

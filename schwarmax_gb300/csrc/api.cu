@@ -46,6 +46,9 @@ int validate_potential(const smx_potential *p) {
                          "needle half-length L must be > 0 (axisymmetric Dehnen models are not built)");
     if (p->bar_a + p->bar_b <= 0 || p->bulge_a + p->bulge_b <= 0 || p->disc_a + p->disc_b <= 0)
         return set_error(SMX_ERR_ARGUMENT, "scale lengths must be > 0");
+    for (int t : {p->bar_type, p->bulge_type})
+        if (!(t == 0 || (t >= 1 && t <= 4) || (t >= 11 && t <= 14)))
+            return set_error(SMX_ERR_UNSUPPORTED, "Dehnen model type %d is not built (T1-T4, V1-V4)", t);
     return SMX_OK;
 }
 

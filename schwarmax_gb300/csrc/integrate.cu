@@ -10,6 +10,7 @@
 // reads each orbit contiguously; consecutive writes of one thread land in the
 // same sectors and merge in L2.
 #include <mutex>
+#include <vector>
 
 #include "smx_internal.cuh"
 
@@ -26,10 +27,10 @@ template <typename T> struct IntegT {
     const int32_t *order;   // queue position -> orbit (NULL: identity)
 };
 
-template <typename T>
+template <typename T, bool CANON>
 __device__ __forceinline__ void rhs(const PotT<T> &P, T om, const T (&y)[6], T (&f)[6]) {
     T p, gx, gy, gz;
-    potential<T, false, true>(P, y[0], y[1], y[2], p, gx, gy, gz);
+    potential<T, false, true, CANON>(P, y[0], y[1], y[2], p, gx, gy, gz);
     f[0] = y[3] + om * y[1];
     f[1] = y[4] - om * y[0];
     f[2] = y[5];
@@ -38,10 +39,10 @@ __device__ __forceinline__ void rhs(const PotT<T> &P, T om, const T (&y)[6], T (
     f[5] = -gz;
 }
 
-template <typename T>
+template <typename T, bool CANON>
 __device__ __forceinline__ T jacobi(const PotT<T> &P, T om, const T (&y)[6]) {
     const T ek = T(0.5) * (y[3] * y[3] + y[4] * y[4] + y[5] * y[5]);
-    return ek + phi_only(P, y[0], y[1], y[2]) - om * (y[0] * y[4] - y[1] * y[3]);
+    return ek + phi_only<T, CANON>(P, y[0], y[1], y[2]) - om * (y[0] * y[4] - y[1] * y[3]);
 }
 
 template <typename T>
@@ -108,7 +109,7 @@ __global__ void __launch_bounds__(128) integrate_init_kernel(PotT<T> P0, T om0, 
 // rates into shared memory, and a lane reads those of its current orbit's point,
 // so that one launch covers the whole batch and the uneven step counts of all its
 // points even out across the SMs.
-template <typename T, bool BATCH>
+template <typename T, bool BATCH, bool CANON>
 __global__ void __launch_bounds__(128) integrate_kernel(PotT<T> P0, IntegT<T> I, const smx_point *__restrict__ points,
                                                        int n_points, int64_t per_point, const T *__restrict__ w0,
                                                        const T *__restrict__ dt0, const T *__restrict__ t_end,
@@ -174,7 +175,7 @@ __global__ void __launch_bounds__(128) integrate_kernel(PotT<T> P0, IntegT<T> I,
 #pragma unroll 1
         for (int s = 0; s < 3; ++s) {
             T f[6];
-            rhs(P, om, yt, f);
+            rhs<T, CANON>(P, om, yt, f);
             if (s == 0) {
 #pragma unroll
                 for (int c = 0; c < 6; ++c) {
@@ -273,7 +274,7 @@ __global__ void __launch_bounds__(128) integrate_kernel(PotT<T> P0, IntegT<T> I,
         if (done) {
             if (sampled && next < n_samp) flags |= 2;
             n_stored[orb] = next < islots ? next : islots;
-            const T EJ = jacobi(P, om, y);
+            const T EJ = jacobi<T, CANON>(P, om, y);
             info[SMX_INFO_T * n_orb + orb] = t;
             info[SMX_INFO_EJ * n_orb + orb] = EJ;
             info[SMX_INFO_WSUM * n_orb + orb] = wsum;
@@ -322,7 +323,18 @@ static int launch(const smx_potential *pot, const smx_integrator *cfg, const smx
     SMX_TRY_CUDA(cudaGetDevice(&dev));
     SMX_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     const size_t smem = points ? (size_t)n_points * sizeof(PointT<T>) : 0;
-    auto kern = points ? integrate_kernel<T, true> : integrate_kernel<T, false>;
+    // the canonical model (T3 bar, V4 bulge) in every point: the compile-time fast path
+    bool canon = true;
+    if (points) {
+        std::vector<smx_point> hp(n_points);
+        SMX_TRY_CUDA(cudaMemcpyAsync(hp.data(), points, n_points * sizeof(smx_point), cudaMemcpyDeviceToHost, s));
+        SMX_TRY_CUDA(cudaStreamSynchronize(s));
+        for (const auto &q : hp) canon = canon && canonical_types(q.pot);
+    } else {
+        canon = canonical_types(*pot);
+    }
+    auto kern = points ? (canon ? integrate_kernel<T, true, true> : integrate_kernel<T, true, false>)
+                       : (canon ? integrate_kernel<T, false, true> : integrate_kernel<T, false, false>);
     if (smem > 48 * 1024) SMX_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
     SMX_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, smem));

@@ -87,6 +87,8 @@ template <typename T> struct PotT {
     T GMd, Md, ad, bd2;                            // Miyamoto-Nagai
     T ba, ba3, bb2, bL, bc1, bc2;                  // T3 bar: c1 = M(1-g)/(2L), c2 = M g/L^2, ba3 = a/3
     T ua, ub2, uL, uc1, uc2;                       // V4 bulge
+    T ua3;                                         // bulge a/3 (for a T3 in the bulge slot)
+    int btype, utype;                              // Dehnen model of each slot (0: T3 / V4)
 };
 
 template <typename T> __host__ __device__ inline PotT<T> make_pot(const smx_potential &p) {
@@ -111,6 +113,9 @@ template <typename T> __host__ __device__ inline PotT<T> make_pot(const smx_pote
     q.uL = T(p.bulge_L);
     q.uc1 = T(p.bulge_M * (1.0 - p.bulge_gamma) / (2.0 * p.bulge_L));
     q.uc2 = T(p.bulge_M * p.bulge_gamma / (p.bulge_L * p.bulge_L));
+    q.ua3 = T(p.bulge_a / 3.0);
+    q.btype = p.bar_type == 0 ? 3 : p.bar_type;
+    q.utype = p.bulge_type == 0 ? 14 : p.bulge_type;
     return q;
 }
 
@@ -223,9 +228,171 @@ __device__ __forceinline__ void needle_sum(T x, T u2, T L, T c1, T c2, const T (
     }
 }
 
+// ----------------------------------------------------- Dehnen-Aly models
+// Potential (and gradient) of one Dehnen & Aly needle model, Phi = -G sum_k kc[k]
+// F_{2k+1} with the coefficients of _make_explicit_fns (dehnen_bar.py:1272-1390):
+// T1..T4 (types 1..4) and V1..V4 (11..14); dk = d kc / dZ with ze = Z - a.  a3 = a/3
+// rounded once in double (the T3 coefficient a (Z - a/3)).
+// FIXED != 0 selects the model at compile time (the canonical fast path of the
+// integrator); FIXED == 0 dispatches on the run-time type.
+template <typename T, bool WANT_PHI, bool WANT_GRAD, int FIXED = 0>
+__device__ __forceinline__ void dehnen_phi(int type_rt, T a, T a3, T b2, T L, T c1, T c2, T x, T y, T z, T &phi, T &gx,
+                                           T &gy, T &gz) {
+    const int type = FIXED ? FIXED : type_rt;
+    if (c1 == T(0) && c2 == T(0)) return;
+    const T G = T(kG);
+    const T ze = M<T>::sqrt_pos(z * z + b2);
+    const T Z = ze + a;
+    const T u2 = y * y + Z * Z;
+    const T aZ = a * Z;
+    const T iz = M<T>::rcp(ze);
+    const T h = T(0.5) * b2;
+    T S0 = T(0), Sx = T(0), Su = T(0), SZ = T(0);
+    switch (type) {
+        case 1: {   // T1 (dehnen_bar.py:1303-1307)
+            const T kc[1] = {T(1)}, dk[1] = {T(0)};
+            needle_sum<T, 1, 0, WANT_GRAD>(x, u2, L, c1, c2, kc, dk, S0, Sx, Su, SZ);
+            break;
+        }
+        case 2: {   // T2 (1309-1316)
+            const T kc[2] = {T(1), aZ}, dk[2] = {T(0), a};
+            needle_sum<T, 2, 0, WANT_GRAD>(x, u2, L, c1, c2, kc, dk, S0, Sx, Su, SZ);
+            break;
+        }
+        case 3: {   // T3 (1318-1326)
+            const T kc[3] = {T(1), a * (Z - a3), aZ * aZ};
+            const T dk[3] = {T(0), a, T(2) * a * aZ};
+            needle_sum<T, 3, 0, WANT_GRAD>(x, u2, L, c1, c2, kc, dk, S0, Sx, Su, SZ);
+            break;
+        }
+        case 4: {   // T4 (1328-1337)
+            const T kc[4] = {T(1), a * (Z - T(0.4) * a), T(0.6) * a * aZ * (Z + Z - a), aZ * aZ * aZ};
+            const T dk[4] = {T(0), a, T(0.6) * a * a * (T(4) * Z - a), T(3) * a * aZ * aZ};
+            needle_sum<T, 4, 0, WANT_GRAD>(x, u2, L, c1, c2, kc, dk, S0, Sx, Su, SZ);
+            break;
+        }
+        case 11: {  // V1 (1339-1346): d(Z/ze)/dZ = -a/ze^2
+            const T kc[2] = {T(1), h * Z * iz}, dk[2] = {T(0), -h * a * iz * iz};
+            needle_sum<T, 2, 0, WANT_GRAD>(x, u2, L, c1, c2, kc, dk, S0, Sx, Su, SZ);
+            break;
+        }
+        case 12: {  // V2 (1348-1357): d(Z^2/ze)/dZ = Z (Z - 2a)/ze^2
+            const T kc[3] = {T(1), aZ + h, T(3) * h * aZ * Z * iz};
+            const T dk[3] = {T(0), a, T(3) * h * a * Z * (Z - a - a) * iz * iz};
+            needle_sum<T, 3, 0, WANT_GRAD>(x, u2, L, c1, c2, kc, dk, S0, Sx, Su, SZ);
+            break;
+        }
+        case 13: {  // V3 (1359-1369): d(Z^3/ze)/dZ = Z^2 (2Z - 3a)/ze^2
+            const T kc[4] = {T(1), a * (Z - a3) + h, aZ * (aZ + T(3) * h), T(5) * h * aZ * aZ * Z * iz};
+            const T dk[4] = {T(0), a, a * (T(2) * aZ + T(3) * h),
+                             T(5) * h * a * a * Z * Z * (T(2) * Z - T(3) * a) * iz * iz};
+            needle_sum<T, 4, 0, WANT_GRAD>(x, u2, L, c1, c2, kc, dk, S0, Sx, Su, SZ);
+            break;
+        }
+        default: {  // 14: V4 (1371-1383)
+            const T kc[5] = {T(1), a * (Z - T(0.4) * a) + h,
+                             T(3) * a * (T(0.2) * aZ * (Z + Z - a) + h * (Z - T(0.2) * a)),
+                             aZ * aZ * (aZ + T(6) * h), T(7) * h * aZ * aZ * aZ * Z * iz};
+            const T dk[5] = {T(0), a, T(3) * a * (T(0.2) * a * (T(4) * Z - a) + h),
+                             a * aZ * (T(3) * aZ + T(12) * h),
+                             T(7) * h * aZ * aZ * aZ * (T(3) * Z - T(4) * a) * iz * iz};
+            needle_sum<T, 5, 0, WANT_GRAD>(x, u2, L, c1, c2, kc, dk, S0, Sx, Su, SZ);
+            break;
+        }
+    }
+    if (WANT_PHI) phi += -G * S0;
+    if (WANT_GRAD) {
+        gx += -G * Sx;
+        gy += -G * Su * T(2) * y;
+        gz += -G * (SZ + Su * T(2) * Z) * (z * iz);
+    }
+}
+
+// Density of one Dehnen & Aly model (dehnen_bar.py:1399-1543): (b^2 / ze^3) pref
+// sum_k kd[k] F_{2k+1}, orders from the first non-zero coefficient.
+template <typename T>
+__device__ __forceinline__ T dehnen_rho(int type, T a, T b2, T L, T c1, T c2, T x, T y, T z) {
+    if (c1 == T(0) && c2 == T(0)) return T(0);
+    const T pi = T(kPi);
+    const T ze = M<T>::sqrt(z * z + b2);
+    const T iz = T(1) / ze;
+    const T Z = ze + a;
+    const T Z2 = Z * Z, A2 = a * a, AZ = a * Z;
+    const T u2 = y * y + Z2;
+    T S0 = T(0), Sx, Su, SZ;
+    T pref;
+    switch (type) {
+        case 1: {
+            const T kd[3] = {T(0), a, T(3) * Z2 * ze}, z0[3] = {T(0), T(0), T(0)};
+            needle_sum<T, 3, 1, false>(x, u2, L, c1, c2, kd, z0, S0, Sx, Su, SZ);
+            pref = T(0.25) / pi;
+            break;
+        }
+        case 2: {
+            const T kd[4] = {T(0), T(0), A2 * a + ze * ze * ze, T(5) * AZ * Z2 * ze}, z0[4] = {};
+            needle_sum<T, 4, 2, false>(x, u2, L, c1, c2, kd, z0, S0, Sx, Su, SZ);
+            pref = T(0.75) / pi;
+            break;
+        }
+        case 3: {
+            const T kd[5] = {T(0), T(0), T(3) * ze * ze * ze, T(5) * a * Z2 * ((T(3) * ze - T(2) * a) * ze + A2),
+                             T(35) * A2 * Z2 * Z2 * ze};
+            const T z0[5] = {};
+            needle_sum<T, 5, 2, false>(x, u2, L, c1, c2, kd, z0, S0, Sx, Su, SZ);
+            pref = T(0.25) / pi;
+            break;
+        }
+        case 4: {
+            const T ze3 = ze * ze * ze;
+            const T kd[6] = {T(0), T(0), T(3) * ze3, T(15) * AZ * ze3, T(7) * A2 * Z * Z2 * ((T(6) * ze - T(3) * a) * ze + A2),
+                             T(63) * A2 * AZ * Z2 * Z2 * ze};
+            const T z0[6] = {};
+            needle_sum<T, 6, 2, false>(x, u2, L, c1, c2, kd, z0, S0, Sx, Su, SZ);
+            pref = T(0.25) / pi;
+            break;
+        }
+        case 11: {
+            const T kd[4] = {T(0), a * iz * iz, T(3) * AZ * iz, T(5) * Z * Z2}, z0[4] = {};
+            needle_sum<T, 4, 1, false>(x, u2, L, c1, c2, kd, z0, S0, Sx, Su, SZ);
+            pref = T(0.375) * b2 / pi;
+            break;
+        }
+        case 12: {
+            const T kd[5] = {T(0), T(0), T(3) * a * A2 * iz * iz, T(5) * Z2 * (ze * ze - T(2) * a * ze + T(3) * A2) * iz,
+                             T(35) * a * Z2 * Z2};
+            const T z0[5] = {};
+            needle_sum<T, 5, 2, false>(x, u2, L, c1, c2, kd, z0, S0, Sx, Su, SZ);
+            pref = T(0.375) * b2 / pi;
+            break;
+        }
+        case 13: {
+            const T ai = a * iz;
+            const T kd[6] = {T(0), T(0), T(0), T(3) * ze * ze * ze * (T(1) + ai * ai * ai * ai * ai),
+                             T(7) * AZ * Z2 * iz * ((T(3) * ze - T(4) * a) * ze + T(3) * A2), T(63) * A2 * Z * Z2 * Z2};
+            const T z0[6] = {};
+            needle_sum<T, 6, 3, false>(x, u2, L, c1, c2, kd, z0, S0, Sx, Su, SZ);
+            pref = T(0.625) * b2 / pi;
+            break;
+        }
+        default: {
+            const T kd[7] = {T(0), T(0), T(0), T(5) * ze * ze * ze,
+                             T(7) * a * Z2 * (T(5) * ze * ze - T(4) * a * ze + T(3) * A2 - T(2) * a * A2 * iz + A2 * A2 * iz * iz),
+                             T(63) * A2 * Z2 * Z2 * (ze + ze - T(2) * a + A2 * iz),
+                             T(231) * A2 * AZ * Z2 * Z2 * Z};
+            const T z0[7] = {};
+            needle_sum<T, 7, 3, false>(x, u2, L, c1, c2, kd, z0, S0, Sx, Su, SZ);
+            pref = T(0.375) * b2 / pi;
+            break;
+        }
+    }
+    return (b2 * iz * iz * iz) * pref * S0;
+}
+
 // ------------------------------------------------------------- potential
 // Phi and/or its gradient (dPhi/dx, ...) of the canonical model at (x, y, z).
-template <typename T, bool WANT_PHI, bool WANT_GRAD>
+// CANON: the bar and bulge slots hold their default models (T3, V4), fixed at
+// compile time; otherwise the slots' types are read from P.
+template <typename T, bool WANT_PHI, bool WANT_GRAD, bool CANON = false>
 __device__ __forceinline__ void potential(const PotT<T> &P, T x, T y, T z, T &phi, T &gx, T &gy, T &gz) {
     const T G = T(kG);
     const T eps = T(kEps);
@@ -259,46 +426,10 @@ __device__ __forceinline__ void potential(const PotT<T> &P, T x, T y, T z, T &ph
             gz += c * s * rz * M<T>::rcp(zeta);
         }
     }
-    {   // T3 bar (dehnen_bar.py:1318-1326)
-        const T a = P.ba;
-        const T ze = M<T>::sqrt_pos(z * z + P.bb2);
-        const T Z = ze + a;
-        const T u2 = y * y + Z * Z;
-        const T aZ = a * Z;
-        const T kc[3] = {T(1), a * (Z - P.ba3), aZ * aZ};
-        const T dk[3] = {T(0), a, T(2) * a * aZ};
-        T S0, Sx, Su, SZ;
-        needle_sum<T, 3, 0, WANT_GRAD>(x, u2, P.bL, P.bc1, P.bc2, kc, dk, S0, Sx, Su, SZ);
-        if (WANT_PHI) phi += -G * S0;
-        if (WANT_GRAD) {
-            gx += -G * Sx;
-            gy += -G * Su * T(2) * y;
-            gz += -G * (SZ + Su * T(2) * Z) * (z * M<T>::rcp(ze));
-        }
-    }
-    {   // V4 bulge (dehnen_bar.py:1371-1383)
-        const T a = P.ua;
-        const T ze = M<T>::sqrt_pos(z * z + P.ub2);
-        const T Z = ze + a;
-        const T u2 = y * y + Z * Z;
-        const T h = T(0.5) * P.ub2;
-        const T aZ = a * Z;
-        const T iz = M<T>::rcp(ze);
-        const T kc[5] = {T(1), a * (Z - T(0.4) * a) + h,
-                         T(3) * a * (T(0.2) * aZ * (Z + Z - a) + h * (Z - T(0.2) * a)),
-                         aZ * aZ * (aZ + T(6) * h), T(7) * h * aZ * aZ * aZ * Z * iz};
-        const T dk[5] = {T(0), a, T(3) * a * (T(0.2) * a * (T(4) * Z - a) + h),
-                         a * aZ * (T(3) * aZ + T(12) * h),
-                         T(7) * h * aZ * aZ * aZ * (T(3) * Z - T(4) * a) * iz * iz};
-        T S0, Sx, Su, SZ;
-        needle_sum<T, 5, 0, WANT_GRAD>(x, u2, P.uL, P.uc1, P.uc2, kc, dk, S0, Sx, Su, SZ);
-        if (WANT_PHI) phi += -G * S0;
-        if (WANT_GRAD) {
-            gx += -G * Sx;
-            gy += -G * Su * T(2) * y;
-            gz += -G * (SZ + Su * T(2) * Z) * (z * iz);
-        }
-    }
+    dehnen_phi<T, WANT_PHI, WANT_GRAD, CANON ? 3 : 0>(P.btype, P.ba, P.ba3, P.bb2, P.bL, P.bc1, P.bc2, x, y, z, phi,
+                                                      gx, gy, gz);
+    dehnen_phi<T, WANT_PHI, WANT_GRAD, CANON ? 14 : 0>(P.utype, P.ua, P.ua3, P.ub2, P.uL, P.uc1, P.uc2, x, y, z, phi,
+                                                       gx, gy, gz);
 }
 
 // Stellar density MN + T3 + V4 (potentials.py:29-49, dehnen_bar.py:1425-1438, 1526-1543).
@@ -317,44 +448,21 @@ __device__ __forceinline__ T density(const PotT<T> &P, T x, T y, T z) {
         const T den = beta * beta * beta * D2 * D2 * M<T>::sqrt(D2);
         rho = (P.bd2 * P.Md / (T(4) * pi)) * (num / den);
     }
-    {   // T3: orders 5, 7, 9 -> K = 5, first used index 2
-        const T a = P.ba, b2 = P.bb2;
-        const T ze = M<T>::sqrt(z * z + b2);
-        const T iz = T(1) / ze;
-        const T Z = ze + a;
-        const T Z2 = Z * Z, A2 = a * a;
-        const T u2 = y * y + Z2;
-        const T kc[5] = {T(0), T(0), T(3) * ze * ze * ze, T(5) * a * Z2 * ((T(3) * ze - T(2) * a) * ze + A2),
-                         T(35) * A2 * Z2 * Z2 * ze};
-        const T dk[5] = {T(0), T(0), T(0), T(0), T(0)};
-        T S0, Sx, Su, SZ;
-        needle_sum<T, 5, 2, false>(x, u2, P.bL, P.bc1, P.bc2, kc, dk, S0, Sx, Su, SZ);
-        rho += (b2 * iz * iz * iz) * (T(0.25) / pi) * S0;
-    }
-    {   // V4: orders 7, 9, 11, 13 -> K = 7, first used index 3
-        const T a = P.ua, b2 = P.ub2;
-        const T ze = M<T>::sqrt(z * z + b2);
-        const T iz = T(1) / ze;
-        const T Z = ze + a;
-        const T Z2 = Z * Z, A2 = a * a, AZ = a * Z;
-        const T u2 = y * y + Z2;
-        const T kc[7] = {T(0), T(0), T(0), T(5) * ze * ze * ze,
-                         T(7) * a * Z2 * (T(5) * ze * ze - T(4) * a * ze + T(3) * A2 - T(2) * a * A2 * iz + A2 * A2 * iz * iz),
-                         T(63) * A2 * Z2 * Z2 * (ze + ze - T(2) * a + A2 * iz),
-                         T(231) * A2 * AZ * Z2 * Z2 * Z};
-        const T dk[7] = {T(0), T(0), T(0), T(0), T(0), T(0), T(0)};
-        T S0, Sx, Su, SZ;
-        needle_sum<T, 7, 3, false>(x, u2, P.uL, P.uc1, P.uc2, kc, dk, S0, Sx, Su, SZ);
-        rho += (b2 * iz * iz * iz) * (T(0.375) * b2 / pi) * S0;
-    }
+    rho += dehnen_rho<T>(P.btype, P.ba, P.bb2, P.bL, P.bc1, P.bc2, x, y, z);
+    rho += dehnen_rho<T>(P.utype, P.ua, P.ub2, P.uL, P.uc1, P.uc2, x, y, z);
     return rho;
 }
 
-template <typename T>
+template <typename T, bool CANON = false>
 __device__ __forceinline__ T phi_only(const PotT<T> &P, T x, T y, T z) {
     T p, a, b, c;
-    potential<T, true, false>(P, x, y, z, p, a, b, c);
+    potential<T, true, false, CANON>(P, x, y, z, p, a, b, c);
     return p;
+}
+
+// true when both Dehnen slots hold their default models
+inline bool canonical_types(const smx_potential &p) {
+    return (p.bar_type == 0 || p.bar_type == 3) && (p.bulge_type == 0 || p.bulge_type == 14);
 }
 
 }  // namespace smx

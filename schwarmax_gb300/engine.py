@@ -43,6 +43,7 @@ class Settings:
     precision: str = "mixed"         # "mixed" (FP32 orbits, split tensor-core NNLS) or "fp64"
     order_probe: bool = False        # sampled mode: order the orbits by the cost of a one-period probe
     nnls: str = None                 # "mixed" / "fp64" NNLS independently of the orbits (None: follow precision)
+    autotune: bool = False           # batched evaluations: tuned integrator launch (autotune.py, cached)
 
     @property
     def dtype(self):
@@ -395,8 +396,17 @@ def evaluate_batch(pots, barys, dd: DeviceData, grid: Grid, st: Settings, nnls_m
             tt[sl] = ic["t_total"]
             dt0[sl] = ic["dt_init"]
         pts = kernels.points_tensor(pots[c0:c1], [-float(b["Omega_bar"]) for b in barys[c0:c1]], w0.device)
+        bps, order = blocks_per_sm, None
+        if st.autotune and mode == SMX_MODE_SAMPLED:
+            from . import autotune
+            tuned = autotune.lookup(Pc * pp, st.n_samples, st.rtol) or \
+                autotune.tune_integrator(pts, Pc, pp, w0, dt0, tt, st)
+            bps = tuned["blocks_per_sm"]
+            if tuned["order"] == "cost":
+                order = autotune.cost_order(pts, Pc, pp, w0, dt0, tt, st)
+        cfg.order = 0 if order is None else order.data_ptr()
         bufs = _integrator_buffers(Pc * pp, st.slots, dtype, role="batch")
-        kernels.integrate_batch(pts, Pc, pp, cfg, w0, dt0, tt, bufs, blocks_per_sm)
+        kernels.integrate_batch(pts, Pc, pp, cfg, w0, dt0, tt, bufs, bps)
         geo = binning_geometry(barys[c0], grid, dd, n_real)
         rots = torch.as_tensor(np.stack([rotation_matrix(b["alpha"], b["beta"], b["gamma"]).reshape(-1)
                                          for b in barys[c0:c1]]), dtype=torch.float64, device="cuda").contiguous()

@@ -19,7 +19,7 @@ import torch
 
 from . import engine, kernels
 from .engine import KPCGYR_TO_KMS, Grid, device_data, settings_from, split_maps
-from .potentials import potential_struct, require_canonical
+from .potentials import model_types, potential_struct, require_canonical
 
 _DEF_NGRID = (10, 6, 6)
 _DEF_LIM = ((0, 10.0), (-3, 3), (-math.pi, math.pi))
@@ -60,7 +60,8 @@ def build_model(density_func, potential_func, params_halo_pot, params_disk_rho, 
     dd = device_data(dict_data, st.n_real)
     if int(num_Vbin) != dd.n_bins:
         raise ValueError(f"num_Vbin={num_Vbin} does not match dict_data ({dd.n_bins} bins)")
-    pot = potential_struct(params_disk_rho, params_halo_pot, st.bulge_mass)
+    pot = potential_struct(params_disk_rho, params_halo_pot, st.bulge_mass,
+                           **model_types(density_func, potential_func))
     r = engine.evaluate(pot, params_disk_rho, dd, grid, st, nnls_maxiter, regularization)
     out = dict(density_3d=r["data"]["y_rz"])
     out.update(split_maps(r["maps"], r["n_cells"], r["n_bins"]))
@@ -80,7 +81,8 @@ def get_model_with_orbit(density_func, potential_func, params_halo_pot, params_d
     st = settings_from(settings)
     grid = _grid(Rzphi_n_grid, Rzphi_lim_grid, xy_lim_grid, xy_n_grid)
     dd = device_data(dict_data, st.n_real)
-    pot = potential_struct(params_disk_rho, params_halo_pot, st.bulge_mass)
+    pot = potential_struct(params_disk_rho, params_halo_pot, st.bulge_mass,
+                           **model_types(density_func, potential_func))
     r = engine.evaluate(pot, params_disk_rho, dd, grid, st, nnls_maxiter, regularization, weights=(1.0, 1.0, 1.0),
                         trajectory=True)
     bufs = r["lib"]["bufs"]
@@ -110,9 +112,19 @@ def model_deltaChi2_jackknife(density_func, potential_func, chi2_func, params_ha
     st = settings_from(settings)
     grid = _grid(Rzphi_n_grid, Rzphi_lim_grid, xy_lim_grid, xy_n_grid)
     dd = device_data(dict_data, st.n_real)
-    pot = potential_struct(params_disk_rho, params_halo_pot, st.bulge_mass)
+    pot = potential_struct(params_disk_rho, params_halo_pot, st.bulge_mass,
+                           **model_types(density_func, potential_func))
     libd = engine.build_library(pot, params_disk_rho, dd, grid, st)
-    lib = libd["library"]
+    return jackknife_of_library(chi2_func, libd["library"], pot, params_disk_rho, dd, grid, st, nnls_maxiter,
+                                regularization, n_groups)
+
+
+def jackknife_of_library(chi2_func, lib, pot, params_disk_rho, dd, grid, st, nnls_maxiter=200, regularization=1.0,
+                         n_groups=100):
+    """The leave-group-out part of model_deltaChi2_jackknife (model.py:480-603) on a
+    library that is already built (for instance one of a batch of parameter points).
+    Mixed precision with groups of at most 8 bins: all replicates in one batched solve;
+    otherwise one solve per replicate."""
     n = lib.shape[0]
     nc, nb = grid.n_cells, dd.n_bins
     y_rz_raw = kernels.density_target(pot, st.dtype, dd.R_grid, dd.z_grid, dd.phi_grid, dd.dR, dd.dz, dd.dphi,

@@ -16,16 +16,31 @@ the bar mass unless ``bulge_mass`` is given.
 """
 import torch
 
-from . import kernels
+from . import _lib, kernels
 from ._lib import SmxPotential
 
 V4_A, V4_B, V4_L, V4_GAMMA = 0.5, 0.5, 0.1, 0.0
 GAMMA_BAR = 1.0
 
 
-def potential_struct(params_baryon, params_halo, bulge_mass=None):
+DEHNEN_TYPES = _lib.DEHNEN_TYPES
+
+
+def _type_code(t, default):
+    if t is None:
+        return 0
+    if isinstance(t, str):
+        if t not in DEHNEN_TYPES:
+            raise NotImplementedError(f"Dehnen model {t} is not built (T1-T4, V1-V4)")
+        return 0 if DEHNEN_TYPES[t] == default else DEHNEN_TYPES[t]
+    return int(t)
+
+
+def potential_struct(params_baryon, params_halo, bulge_mass=None, bar_type=None, bulge_type=None):
     """Reference parameter dicts -> smx_potential.  Shifted or tilted components
-    (potentials.py:8-15) are not part of the canonical model."""
+    (potentials.py:8-15) are not part of the canonical model.  bar_type / bulge_type
+    ("T1".."T4", "V1".."V4", default T3 / V4) choose another Dehnen & Aly model
+    (dehnen_bar.py:1272-1555) for either slot."""
     for p in (params_baryon, params_halo):
         for k in ("x_origin", "y_origin", "z_origin", "dirx", "diry"):
             if k in p and float(p[k]) != 0.0:
@@ -42,14 +57,21 @@ def potential_struct(params_baryon, params_halo, bulge_mass=None):
         bar_M=m_bar, bar_a=float(params_baryon["a_bar"]), bar_b=float(params_baryon["b_bar"]),
         bar_L=float(params_baryon["L_bar"]), bar_gamma=GAMMA_BAR,
         bulge_M=m_bar if bulge_mass is None else float(bulge_mass), bulge_a=V4_A, bulge_b=V4_B, bulge_L=V4_L,
-        bulge_gamma=V4_GAMMA)
+        bulge_gamma=V4_GAMMA, bar_type=_type_code(bar_type, 3), bulge_type=_type_code(bulge_type, 14))
 
 
 class _Canonical:
     kind = None
 
+    def __init__(self, bar_type="T3", bulge_type="V4"):
+        self.bar_type, self.bulge_type = bar_type, bulge_type
+
+    @property
+    def types(self):
+        return dict(bar_type=self.bar_type, bulge_type=self.bulge_type)
+
     def __repr__(self):
-        return f"<schwarmax_gb300 canonical {self.kind}>"
+        return f"<schwarmax_gb300 {self.kind} (bar {self.bar_type}, bulge {self.bulge_type})>"
 
 
 class DensityFunc(_Canonical):
@@ -57,7 +79,7 @@ class DensityFunc(_Canonical):
     kind = "density_func"
 
     def __call__(self, x, y, z, params):
-        pot = potential_struct(params, dict(logM=0.0, Rs=1.0))
+        pot = potential_struct(params, dict(logM=0.0, Rs=1.0), **self.types)
         return kernels.potential_eval(pot, x, y, z, want_phi=False, want_acc=False, want_rho=True)["rho"]
 
 
@@ -66,12 +88,12 @@ class PotentialFunc(_Canonical):
     kind = "potential_func"
 
     def __call__(self, x, y, z, params_baryon, params_halo):
-        pot = potential_struct(params_baryon, params_halo)
+        pot = potential_struct(params_baryon, params_halo, **self.types)
         return kernels.potential_eval(pot, x, y, z, want_phi=True, want_acc=False)["phi"]
 
     def acceleration(self, x, y, z, params_baryon, params_halo):
         """-grad Phi (the reference's acc_fn, model.py:152-157) as a (3, n) tensor."""
-        pot = potential_struct(params_baryon, params_halo)
+        pot = potential_struct(params_baryon, params_halo, **self.types)
         return kernels.potential_eval(pot, x, y, z, want_phi=False, want_acc=True)["acc"]
 
 
@@ -79,11 +101,31 @@ density_func = DensityFunc()
 potential_func = PotentialFunc()
 
 
+def dehnen_model(bar="T3", bulge="V4"):
+    """(density_func, potential_func) of the model NFW + MN + a Dehnen & Aly bar of type
+    `bar` + a bulge of type `bulge` (any of T1..T4, V1..V4; the reference builds such
+    models from dehnen_bar.py's T*_potential / V*_potential functions).  The pair is
+    accepted by build_model, get_model_with_orbit and model_deltaChi2_jackknife like the
+    canonical one."""
+    for t in (bar, bulge):
+        _type_code(t, 0)
+    return DensityFunc(bar, bulge), PotentialFunc(bar, bulge)
+
+
+def model_types(density, potential):
+    """bar_type / bulge_type of a descriptor pair (they must agree)."""
+    if density is not None and potential is not None and density.types != potential.types:
+        raise ValueError("density_func and potential_func describe different Dehnen models")
+    d = potential if potential is not None else density
+    return d.types if d is not None else {}
+
+
 def require_canonical(density, potential):
     if density is not None and not isinstance(density, DensityFunc):
-        raise NotImplementedError("only the canonical density_func (MN + T3 + V4) has a GB300 kernel")
+        raise NotImplementedError("only the descriptor density_func (MN + Dehnen bar + bulge) has a GB300 kernel")
     if potential is not None and not isinstance(potential, PotentialFunc):
-        raise NotImplementedError("only the canonical potential_func (NFW + MN + T3 + V4) has a GB300 kernel")
+        raise NotImplementedError("only the descriptor potential_func (NFW + MN + Dehnen bar + bulge) has a GB300 "
+                                  "kernel")
 
 
 def as_cuda(x, dtype):

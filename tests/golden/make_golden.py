@@ -411,6 +411,37 @@ def case_example_jackknife():
     save("example_jackknife", theta=g["theta"], delta_chi2=np.array(dchi2))
 
 
+def case_dehnen_types():
+    """Potential, density and -grad Phi (jax.grad) of every Dehnen & Aly model T1..T4 and
+    V1..V4 of the reference (dehnen_bar.py:1272-1568), each with its own (M, a, b, L,
+    gamma), at 64 points."""
+    import dehnen_bar as db
+    rng = np.random.default_rng(9)
+    out = {}
+    specs = {"T1": (1e10, 0.8, 0.3, 3.0, 0.4), "T2": (2e10, 1.0, 0.4, 4.0, 1.0), "T3": (1e10, 0.8, 0.3, 4.0, 0.7),
+             "T4": (1.5e10, 0.6, 0.5, 2.5, 0.0), "V1": (5e9, 0.5, 0.6, 0.4, 0.3), "V2": (5e9, 0.4, 0.5, 0.1, 0.0),
+             "V3": (8e9, 0.7, 0.3, 1.5, 0.5), "V4": (5e9, 0.5, 0.5, 0.1, 0.0)}
+    for name, (M, a, b, L, gam) in specs.items():
+        fphi = getattr(db, name + "_potential")
+        frho = getattr(db, name + "_density")
+        x = rng.uniform(-8, 8, 64)
+        y = rng.uniform(-6, 6, 64)
+        z = rng.uniform(-2, 2, 64)
+        x[:3] = [0.05, 3.0, -9.0]
+        y[:3] = [0.0, 0.01, 1.0]
+        z[:3] = [0.0, -0.02, 0.5]
+        phi = np.array([float(fphi(x[i], y[i], z[i], M, a, b, L, gam)) for i in range(64)])
+        rho = np.array([float(frho(x[i], y[i], z[i], M, a, b, L, gam)) for i in range(64)])
+
+        def _p(pos, f=fphi, M=M, a=a, b=b, L=L, gam=gam):
+            return f(pos[0], pos[1], pos[2], M, a, b, L, gam)
+
+        acc = np.stack([-jax.grad(_p)(jnp.array([x[i], y[i], z[i]])) for i in range(64)])
+        out.update({f"{name}_params": np.array([M, a, b, L, gam]), f"{name}_x": x, f"{name}_y": y, f"{name}_z": z,
+                    f"{name}_phi": phi, f"{name}_rho": rho, f"{name}_acc": acc})
+    save("dehnen_types", **out)
+
+
 def case_analysis():
     """build_Lcirc_of_E (utils.py:275-341) of the canonical potential on a 400-point
     table with its interpolator at a set of energies, and compute_transfer_matrix

@@ -179,3 +179,52 @@ def test_calculate_delta_chi2_batched_matches_loop(small):
     got = model.model_deltaChi2_jackknife(density_func, potential_func, chi2_func, halo, bary, dd, cfg.n_bins, nc,
                                           settings=st_b, **kw)
     assert abs(float(got) - float(ref)) <= 1e-6 * abs(float(ref)) + 1e-9, (float(got), float(ref))
+
+
+def test_mixed_solver_at_config4_geometry():
+    """The large-library geometry of config 4 (120 x 120 pixels, 1,500 apertures, a
+    32 x 32 x 16 grid: 16,384 + 5 x 1,500 = 23,884 design rows, 25,384 library rows)
+    with a reduced orbit count: the NNLS workspace, the shared-memory histogram row
+    (25,384 int64 = 203 KB) and the Newton-Schulz inverse of a 23,884^2 G at that size,
+    against the FP64 solver on the same library."""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from schwarmax_gb300 import engine, kernels, synthetic
+    from schwarmax_gb300.likelihood import log_likelihoods
+    cfg = synthetic.Config("config4-geometry", n_part=8192, n_samples=100, n_pix=120, n_bins=1500,
+                           n_grid=(32, 32, 16), n_boot=10, n_periods=5.0, n_real=1, bar_mass=2e10,
+                           omega_kms_kpc=40.0)
+    dd, theta = synthetic.make_dataset(cfg, seed=2)
+    st = cfg.settings("mixed")
+    ddv = engine.DeviceData(dd, n_real=st.n_real)
+    nc = 32 * 32 * 16
+    logl_m, r = log_likelihoods(theta, ddv, cfg.n_bins, nc, settings=st, nnls_maxiter=50)
+    lib = r["lib"]["library"]
+    assert lib.shape == (8192, nc + 6 * 1500)
+    d = r["data"]
+    row_scale, Y = engine.nnls_inputs(d, ddv, nc, (math.sqrt(5.0), math.sqrt(5.0), 1.0))
+    assert Y.shape == (10, nc + 5 * 1500)
+    w_init = float((d["y_rz"].sum() / lib.shape[0]).item())
+    W64 = kernels.nnls_admm(lib.double(), engine.row_map(nc, cfg.n_bins), row_scale, Y, 50, 1.0, w_init, mixed=False)
+    y_xy_b, y_h_b, sh = engine.likelihood_data(ddv)
+    lum = float(d["mmpo"].item()) * d["l2m"]
+    _, logl_64 = kernels.model_maps(lib.double(), nc, cfg.n_bins, W64, d["gamma"].contiguous(), ddv.v0, ddv.s,
+                                    d["y_rz"].contiguous(), ddv.xy, y_xy_b, y_h_b, sh, lum, 1.0, want_maps=False)
+    assert float((2 * (logl_m - logl_64)).abs().max()) <= 0.05
+    assert float((r["W"] - W64).abs().max() / W64.abs().max()) <= 1e-6
+
+
+def test_autotuned_batch_gives_the_same_results(small, tmp_path, monkeypatch):
+    """The tuner's launch choices (blocks per SM, queue order) change no result; its
+    choice is cached."""
+    from schwarmax_gb300 import autotune
+    from schwarmax_gb300.likelihood import log_likelihoods_batch
+    monkeypatch.setattr(autotune, "CACHE", str(tmp_path / "autotune.json"))
+    cfg, dd, thetas = small
+    st = cfg.settings("fp64")
+    nc = int(np.prod(cfg.n_grid))
+    a, _ = log_likelihoods_batch(thetas, dd, cfg.n_bins, nc, settings=st, nnls_maxiter=40)
+    st.autotune = True
+    b, _ = log_likelihoods_batch(thetas, dd, cfg.n_bins, nc, settings=st, nnls_maxiter=40)
+    np.testing.assert_allclose(a.cpu().numpy(), b.cpu().numpy(), rtol=1e-12)
+    assert autotune.load()

@@ -208,3 +208,22 @@ def test_jackknife_on_the_example_galaxy():
     d = likelihood.calculate_delta_chi2(j["theta"], dd, dd["total_bins"], dd["Rzphi_n_tot"])
     ref = float(j["delta_chi2"])
     assert abs(d - ref) <= 1e-4 * abs(ref), (d, ref)
+
+
+@pytest.mark.parametrize("name", ["T1", "T2", "T3", "T4", "V1", "V2", "V3", "V4"])
+def test_dehnen_models_match_reference(name):
+    """Every Dehnen & Aly model of the reference (T1..T4, V1..V4): potential, density and
+    -grad Phi against the reference's own functions (jax.grad by complex step)."""
+    from oracle import dual as Dd, potential as op
+    g = golden("dehnen_types")
+    M, a, b, L, gam = g[name + "_params"]
+    x, y, z = g[name + "_x"], g[name + "_y"], g[name + "_z"]
+    code = op.DEHNEN_CODES[name]
+    phi = op.DEHNEN_PHI[code](x, y, z, M, a, b, L, gam)
+    rho = op.DEHNEN_RHO[code](x, y, z, M, a, b, L, gam)
+    np.testing.assert_allclose(phi, g[name + "_phi"], rtol=1e-11, atol=0)
+    np.testing.assert_allclose(rho, g[name + "_rho"], rtol=1e-9, atol=1e-12 * np.abs(g[name + "_rho"]).max())
+    X, Y, Z = Dd.seed(x, y, z)
+    p = op.DEHNEN_PHI[code](X, Y, Z, M, a, b, L, gam)
+    acc = -np.stack([p.d[0], p.d[1], p.d[2]], -1)
+    np.testing.assert_allclose(acc, g[name + "_acc"], rtol=1e-9, atol=1e-10 * np.abs(g[name + "_acc"]).max())
