@@ -43,9 +43,11 @@ def test_dehnen_model_matches_reference(kern, name, slot):
     np.testing.assert_allclose(out["acc"].cpu().numpy(), acc, rtol=1e-9, atol=1e-10 * np.abs(acc).max())
     rho = g[name + "_rho"]
     np.testing.assert_allclose(out["rho"].cpu().numpy(), rho, rtol=1e-8, atol=1e-11 * np.abs(rho).max())
-    # FP32: the same formulas in single precision
+    # FP32: the same formulas in single precision.  The needle sums alternate in sign
+    # (V1 reaches 6e-5 relative at 2 of the 64 points, a cancellation of about 1,000
+    # float ulp), so Phi gets 1.5e-4; the forces that drive the orbits keep 2e-3 of |a|.
     o32 = kern.potential_eval(pot, x.float(), y.float(), z.float(), want_phi=True, want_acc=True)
-    np.testing.assert_allclose(o32["phi"].double().cpu().numpy(), g[name + "_phi"], rtol=5e-5)
+    np.testing.assert_allclose(o32["phi"].double().cpu().numpy(), g[name + "_phi"], rtol=1.5e-4)
     np.testing.assert_allclose(o32["acc"].double().cpu().numpy(), acc, rtol=2e-3, atol=2e-4 * np.abs(acc).max())
 
 
