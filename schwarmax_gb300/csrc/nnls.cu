@@ -9,7 +9,8 @@
 // w = (Q + rho I)^-1 (rho d + U^T y) is evaluated in residual form
 //   w = k d + U^T G^-1 (y - k U d),   k = rho/c,
 // which costs two skinny GEMMs with U and one application of G^-1 per
-// iteration.  The grouping matters in low precision: the algebraically equal
+// iteration.  The mixed path forms H = G^-1 U once per solve and iterates
+// w = D + H^T (y - U D): two skinny products per iteration (U D and H^T E).  The grouping matters in low precision: the algebraically equal
 // k (d - U^T G^-1 U d) + U^T G^-1 y subtracts two vectors of the size of d whose
 // difference is up to cond(G) times smaller, so rounding errors of G^-1 and of
 // the products grow by cond(G) (about 1.8e3 at 16384 orbits); in residual form
@@ -21,9 +22,10 @@
 // SMX_NNLS_MIXED: U in float; every product on the bf16 tensor cores with
 // FP64-grade accuracy by Ozaki splitting (split_gemm.cuh): U in 4 slices (31 bits
 // below each row's or column's largest magnitude), the iterates' vectors in 5
-// (39 bits), G^-1 in 5.  G = U U^T + cI is formed from the slices of U; G^-1
-// starts from a float Cholesky inverse and is refined by Newton-Schulz steps
-// whose residual products use 7 slices; the iterates z, u, D stay in double.
+// (39 bits), G^-1 in 5, H = G^-1 U in 4.  G = U U^T + cI is formed from the slices
+// of U; G^-1 starts from a float Gauss-Jordan inverse and is refined by
+// Newton-Schulz steps whose residual products use 7 slices; the iterates z, u, D
+// stay in double.
 // At 16384 orbits (cond(G) = 1.8e3) the weights move the chi^2 by about 0.02
 // when U is rounded to float, by about 40 when G^-1 is stored in float and by
 // about 500 when the iterations run in float arithmetic, which is why the
@@ -123,7 +125,9 @@ struct Layout {
     int lwork;
 };
 
-static int layout(const smx_nnls_problem *p, Layout *L, cusolverDnHandle_t solver) {
+// with_h: the bootstrap solver's accumulators also hold the m x n product O U that
+// forms H = G^-1 U once per solve (the jackknife applies its own inverses and does not)
+static int layout(const smx_nnls_problem *p, Layout *L, cusolverDnHandle_t solver, bool with_h = true) {
     const size_t m = p->m, n = p->n, B = p->n_rhs;
     const bool mixed = p->mode == SMX_NNLS_MIXED;
     size_t off = 0;
@@ -156,6 +160,7 @@ static int layout(const smx_nnls_problem *p, Layout *L, cusolverDnHandle_t solve
         const SplitShapes sh = split_shapes(p);
         const size_t mx = m > n ? m : n;
         L->acc_elems = (int64_t)(m * m > mx * B ? m * m : mx * B);
+        if (with_h && (int64_t)(m * n) > L->acc_elems) L->acc_elems = (int64_t)(m * n);
         L->Tacc = take(L->acc_elems * sizeof(unsigned long long));
         L->Racc = take(L->acc_elems * sizeof(float));
         L->rowmax = take(mx * sizeof(unsigned long long));
@@ -295,6 +300,8 @@ enum { COL_INIT = 0, COL_RESID = 1, COL_PLAIN = 2, COL_UPDATE = 3 };
 constexpr int kNsMaxSteps = 5;   // Newton-Schulz steps at most (a seed residual of 0.2 needs 4)
 
 constexpr int VS = 5;          // slices of the vector operands: 39 bits below each column's largest magnitude
+// slice pairs (s, t) of the skinny products U D, H^T E (jackknife: U^T F) with s + t <= kSkinnyLevels
+constexpr int kSkinnyLevels = 7;
 constexpr int COL_CHUNK = 1024;   // k per CTA of the column kernels
 
 struct ColArgs {
@@ -552,6 +559,18 @@ __global__ void clear_kernel(unsigned long long *T, float *R, int64_t count) {
     }
 }
 
+// H = G^-1 U = diag(g) U + O U in place of U (both m x n column-major): the product
+// O U arrives as T, R with row exponents of O and column exponents of U; T, R cleared.
+__global__ void h_combine_kernel(unsigned long long *T, float *R, const int32_t *eO, const int32_t *eU,
+                                 const double *g, double *U, int64_t m, int64_t n) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < m * n; k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = k % m, i = k / m;
+        U[k] = g[r] * U[k] + product_value(T, R, k, eO[r], eU[i]);
+        T[k] = 0ull;
+        R[k] = 0.0f;
+    }
+}
+
 // The set-up of the mixed path shared by the bootstrap and jackknife solvers: U in
 // double, ||U||_F^2 and the ADMM coefficient, U sliced both ways, G = U U^T + c I
 // from the slices, G^-1 by a float seed and Newton-Schulz steps, and G^-1 split into
@@ -566,7 +585,8 @@ struct MixedState {
 
 template <typename TL>
 static int mixed_setup(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map, const double *row_scale,
-                       unsigned char *ws, const Layout &L, Handles *h, cudaStream_t s, MixedState &S) {
+                       unsigned char *ws, const Layout &L, Handles *h, cudaStream_t s, MixedState &S,
+                       bool make_h = false) {
     const int64_t m = p->m, n = p->n;
     const double lam = p->lambda_reg;
     double *G = (double *)(ws + L.G);
@@ -630,8 +650,9 @@ static int mixed_setup(const smx_nnls_problem *p, const TL *lib, const int32_t *
     //   R = I - G X (diagonals exact, off-diagonal parts as a 7 x 7 split
     //   product), X <- X + X R.
     // The new X has residual R^2, whose 2-norm is at most ||R||_F^2: steps
-    // continue until a step's input has ||R||_F <= 3e-7, so the result has
-    // ||I - G X|| <= 1e-13 up to the accuracy of G X times cond(G) (about 2^-44).
+    // continue until a step's input has ||R||_F <= 1e-5, so the result has
+    // ||I - G X|| <= 1e-10 and X a relative error of at most 1e-10 (a float seed
+    // with ||R||_F ~ 2e-3 needs two steps: 2e-3 -> 4e-6 -> 1.6e-11).
     // The stopping rule runs on the device (ns_gate_kernel): the kernels of a step
     // that is not needed return at once, and nothing is read back here.
     const int64_t mp = spd_inverse_padded(m);
@@ -651,7 +672,7 @@ static int mixed_setup(const smx_nnls_problem *p, const TL *lib, const int32_t *
         if ((st = split::gemm(sh.G7, sh.X7, acc, false, derr, s, 0, skip))) return st;
         SMX_TRY_CUDA(cudaMemsetAsync(rss, 0, sizeof(double), s));
         ns_residual_kernel<<<grid1d(m * m), 256, 0, s>>>(Tacc, Racc, sh.G7.expo, sh.X7.expo, G, Xd, Rd, m, rss, skip);
-        ns_gate_kernel<<<1, 1, 0, s>>>(rss, 9e-14, nsf);
+        ns_gate_kernel<<<1, 1, 0, s>>>(rss, 1e-10, nsf);
         count_launch(2);
         if ((st = split::slice_rows<double>(Xd, 1, m, sh.X5, rowmax, s, false, skip))) return st;   // X rows over k
         if ((st = split::slice_rows<double>(Rd, m, 1, sh.R5, rowmax, s, false, skip))) return st;   // R columns over k
@@ -666,6 +687,16 @@ static int mixed_setup(const smx_nnls_problem *p, const TL *lib, const int32_t *
     split_diag_kernel<<<grid1d(m), 256, 0, s>>>(Xd, gdiag, m);
     count_launch();
     if ((st = split::slice_rows<double>(Xd, 1, m, sh.Xg, rowmax, s))) return st;   // O rows over columns
+    if (make_h) {
+        // H = G^-1 U, once per solve: every iteration then needs U D and H^T E only
+        // (w = D + H^T (y - U D)), in place of U D, G^-1 E and U^T F.  U is overwritten
+        // by H, and the slices of U^T (orbits over rows) by those of H^T.
+        split::Acc acc_h{Tacc, Racc, m};
+        if ((st = split::gemm(sh.Xg, sh.Ut, acc_h, false, derr, s))) return st;   // O U
+        h_combine_kernel<<<grid1d(m * n), 256, 0, s>>>(Tacc, Racc, sh.Xg.expo, sh.Ut.expo, gdiag, U, m, n);
+        count_launch();
+        if ((st = split::slice_rows<double>(U, m, 1, sh.Ut, rowmax, s))) return st;   // H^T: orbits over rows
+    }
     S.sh = sh;
     S.Tacc = Tacc;
     S.Racc = Racc;
@@ -726,7 +757,7 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
     } else {
         MixedState S;
         int st;
-        if ((st = mixed_setup<TL>(p, lib, row_map, row_scale, ws, L, h, s, S))) return st;
+        if ((st = mixed_setup<TL>(p, lib, row_map, row_scale, ws, L, h, s, S, true))) return st;
         SplitShapes &sh = S.sh;
         unsigned long long *Tacc = S.Tacc;
         float *Racc = S.Racc;
@@ -734,11 +765,10 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
         double *gdiag = S.gdiag, *Ebuf = (double *)(ws + L.Ebuf);
         double *Z = (double *)(ws + L.Z), *Uu = (double *)(ws + L.Uu), *D = (double *)(ws + L.D);
         const double *coefp = frob + 1;
-        // column maxima of the three vector operands (D, E, F), cleared once here and
+        // column maxima of the two vector operands (D, E), cleared once here and
         // afterwards by the phase-1 kernel of the operand that follows each one
-        unsigned long long *cmD = (unsigned long long *)(ws + L.colmax), *cmE = cmD + B, *cmF = cmE + B;
+        unsigned long long *cmD = (unsigned long long *)(ws + L.colmax), *cmE = cmD + B;
         SMX_TRY_CUDA(cudaMemsetAsync(cmD, 0, 3 * B * sizeof(unsigned long long), s));
-        double *Fbuf = (double *)(ws + L.Fbuf);
         auto col = [&](int mode, int64_t K, const int32_t *eA, const int32_t *eB, split::Operand &out,
                        int t_shift) -> int {
             ColArgs a;
@@ -763,19 +793,16 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
             a.slice_elems = out.slice_elems();
             a.tile_rows = out.tile_rows;
             a.t_shift = t_shift;
-            // E follows D, F follows E, D follows F
+            // E follows D, D follows E
             if (mode == COL_RESID) {
                 a.V = Ebuf; a.colmax = cmE; a.reset = cmD;
-            } else if (mode == COL_PLAIN) {
-                a.V = Fbuf; a.colmax = cmF; a.reset = cmE;
             } else {
-                a.V = D; a.colmax = cmD; a.reset = cmF;
+                a.V = D; a.colmax = cmD; a.reset = cmE;
             }
             const dim3 g((unsigned)((K + COL_CHUNK - 1) / COL_CHUNK), (unsigned)B);
             switch (mode) {
                 case COL_INIT: column_values_kernel<COL_INIT><<<g, 256, 0, s>>>(a); break;
                 case COL_RESID: column_values_kernel<COL_RESID><<<g, 256, 0, s>>>(a); break;
-                case COL_PLAIN: column_values_kernel<COL_PLAIN><<<g, 256, 0, s>>>(a); break;
                 default: column_values_kernel<COL_UPDATE><<<g, 256, 0, s>>>(a); break;
             }
             count_launch();
@@ -786,19 +813,17 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
             return SMX_OK;
         };
         split::Acc acc_m{Tacc, Racc, m}, acc_n{Tacc, Racc, n};
-        // U D and U^T F drop the slice pairs s + t >= 8 (U has no dominant
-        // element per row or column: its products sit in the exact levels)
+        // U D and H^T E drop the slice pairs s + t >= 8 (U and H have no dominant
+        // element per row or column: their products sit in the exact levels).
+        // sh.Ut holds the slices of H^T (mixed_setup), E takes the 112-wide operand sh.Fs.
         const int sh_ud = 8 * (split::exact_levels(sh.Ua, sh.Ds) - 1);
-        const int sh_ge = 8 * (split::exact_levels(sh.Xg, sh.Es) - 1);
-        const int sh_uf = 8 * (split::exact_levels(sh.Ut, sh.Fs) - 1);
+        const int sh_he = 8 * (split::exact_levels(sh.Ut, sh.Fs) - 1);
         col(COL_INIT, n, nullptr, nullptr, sh.Ds, 0);
         for (int it = 0; it < p->maxiter; ++it) {
-            if ((st = split::gemm(sh.Ua, sh.Ds, acc_m, false, derr, s, 7))) return st;   // U D
-            col(COL_RESID, m, sh.Ua.expo, sh.Ds.expo, sh.Es, sh_ud);                    // E = Y - U D
-            if ((st = split::gemm(sh.Xg, sh.Es, acc_m, false, derr, s))) return st;   // O E
-            col(COL_PLAIN, m, sh.Xg.expo, sh.Es.expo, sh.Fs, sh_ge);                    // F = g E + O E
-            if ((st = split::gemm(sh.Ut, sh.Fs, acc_n, false, derr, s, 7))) return st;   // U^T F
-            col(COL_UPDATE, n, sh.Ut.expo, sh.Fs.expo, sh.Ds, sh_uf);                   // ADMM update, D
+            if ((st = split::gemm(sh.Ua, sh.Ds, acc_m, false, derr, s, kSkinnyLevels))) return st;   // U D
+            col(COL_RESID, m, sh.Ua.expo, sh.Ds.expo, sh.Fs, sh_ud);                    // E = Y - U D
+            if ((st = split::gemm(sh.Ut, sh.Fs, acc_n, false, derr, s, kSkinnyLevels))) return st;   // H^T E
+            col(COL_UPDATE, n, sh.Ut.expo, sh.Fs.expo, sh.Ds, sh_he);                   // ADMM update, D
         }
         SMX_TRY_CUDA(cudaMemcpyAsync(Z_out, Z, sizeof(double) * n * B, cudaMemcpyDeviceToDevice, s));
         SMX_TRY_CUDA(cudaMemcpyAsync(dinfo + 2, derr, sizeof(int), cudaMemcpyDeviceToDevice, s));
@@ -1150,7 +1175,7 @@ static int run_jackknife(const smx_nnls_problem *p, const TL *lib, const int32_t
         slices(a, sh.Ds);
     }
     for (int it = 0; it < p->maxiter; ++it) {
-        if ((st = split::gemm(sh.Ua, sh.Ds, acc_m, false, S.derr, s, 7))) return st;   // U D
+        if ((st = split::gemm(sh.Ua, sh.Ds, acc_m, false, S.derr, s, kSkinnyLevels))) return st;   // U D
         SMX_TRY_CUDA(cudaMemsetAsync(cmE, 0, B * sizeof(unsigned long long), s));
         {
             ColArgs a = args(m, sh.Ua.expo, sh.Ds.expo, sh.Es, sh_ud, Ebuf, cmE);
@@ -1173,7 +1198,7 @@ static int run_jackknife(const smx_nnls_problem *p, const TL *lib, const int32_t
             count_launch();
             slices(a, out);
         }
-        if ((st = split::gemm(sh.Ut, sh.Fs, acc_n, false, S.derr, s, 7))) return st;   // U^T F
+        if ((st = split::gemm(sh.Ut, sh.Fs, acc_n, false, S.derr, s, kSkinnyLevels))) return st;   // U^T F
         SMX_TRY_CUDA(cudaMemsetAsync(cmD, 0, B * sizeof(unsigned long long), s));
         {
             ColArgs a = args(n, sh.Ut.expo, sh.Fs.expo, sh.Ds, sh_uf, D, cmD);
@@ -1253,7 +1278,7 @@ extern "C" int smx_nnls_jackknife_workspace_size(const smx_nnls_problem *p, int 
     smx_nnls_problem q = *p;
     q.mode = SMX_NNLS_MIXED;
     Layout L;
-    if ((st = layout(&q, &L, h->solver))) return st;
+    if ((st = layout(&q, &L, h->solver, false))) return st;
     *bytes = jk_layout(L.total, p->m, p->n_rhs, max_drop).total;
     return SMX_OK;
 }
@@ -1277,7 +1302,7 @@ extern "C" int smx_nnls_jackknife(const smx_nnls_problem *p, const void *library
     int st = get_handles(s, &h);
     if (st) return st;
     Layout L;
-    if ((st = layout(p, &L, h->solver))) return st;
+    if ((st = layout(p, &L, h->solver, false))) return st;
     const JkLayout J = jk_layout(L.total, p->m, p->n_rhs, max_drop);
     if (workspace_bytes < J.total)
         return set_error(SMX_ERR_WORKSPACE, "smx_nnls_jackknife: workspace %zu < %zu bytes", workspace_bytes, J.total);

@@ -131,7 +131,7 @@ struct Acc {
 int exact_levels(const Operand &A, const Operand &B);
 
 // Launch C += A B^T (A: M x K, B: N x K) into acc.  Supported: 4 or 5 slices
-// per operand with B.tile_rows 112, 4 x 4 or 5 x 5 with 128, 5 x 5 with 64,
+// per operand with B.tile_rows 112, 4 x 4, 5 x 4 or 5 x 5 with 128, 5 x 5 with 64,
 // 7 x 7 with 96.
 // lower_only: only output tiles with column tile <= row tile (symmetric results,
 // requires A.tile_rows == B.tile_rows).  err receives a nonzero code if a wait
