@@ -118,8 +118,7 @@ def run_ours(args, rank, world, local):
 
     import schwarmax_gb300 as smx
     from schwarmax_gb300 import _lib, engine, synthetic
-    from schwarmax_gb300.likelihood import (grid_of, log_likelihoods, log_likelihoods_batch, log_mean_exp,
-                                            unpack_params)
+    from schwarmax_gb300.likelihood import grid_of, log_likelihoods, log_mean_exp, unpack_params
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
@@ -131,24 +130,12 @@ def run_ours(args, rank, world, local):
     dict_data, theta = synthetic.make_dataset(cfg, seed=args.seed)
     setup_s = time.time() - t0
     st = cfg.settings("mixed")
-    st.autotune = bool(getattr(args, "autotune", False))
     dd = engine.DeviceData(dict_data, n_real=st.n_real)
     nb = cfg.n_bins
     nc = cfg.n_grid[0] * cfg.n_grid[1] * cfg.n_grid[2]
     kw = dict(settings=st, nnls_maxiter=cfg.admm_iters)
-    batched = args.config == 2
-    points = synthetic.points_for(cfg, args.points, seed=args.seed) if batched else None
-    evals_per_step = args.points if batched else 1
 
     def step(i, timers=None):
-        if batched:
-            th = points.copy()
-            th[:, 10] = th[:, 10] + 0.002 * ((i % 5) - 2)
-            logl, r = log_likelihoods_batch(th, dd, nb, nc, keep=args.jackknife, **kw)
-            if args.jackknife:
-                r["jackknife"] = jackknife_batch(th, r, dd, nb, st, cfg.admm_iters)
-            m = torch.max(logl, dim=1, keepdim=True).values
-            return m[:, 0] + torch.log(torch.mean(torch.exp(logl - m), dim=1)), r
         th = theta.copy()
         th[10] = theta[10] + 0.002 * ((i % 5) - 2)          # M/L walk, MCMC-like
         logl, r = log_likelihoods(th, dd, nb, nc, **kw)
@@ -164,7 +151,6 @@ def run_ours(args, rank, world, local):
     torch.cuda.synchronize()
     launches0 = _lib.kernel_launches()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    integ_ms = []
     ev0.record()
     for i in range(args.steps):
         val, r = step(i)
@@ -176,28 +162,7 @@ def run_ours(args, rank, world, local):
     ms = max_over_ranks(ev0.elapsed_time(ev1), dev)
     if sampler:
         sampler.terminate()
-    value = whole_job_rate(world, args.steps * evals_per_step, ms)
-    if batched:
-        # --- batched workload: the line reports the batch; no per-kernel extras -----
-        if rank == 0:
-            clocks = clock_summary(os.path.join(args.out, f"clocks_rank{rank}.csv"), local)
-            line = {"metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
-                    "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3), "higher_is_better": True,
-                    "scaling": "weak", "vs_baseline": None,
-                    "dtype": "f32 (orbits, binning) / bf16 split products + f64 (NNLS)",
-                    "data": "synthetic (seeded; schwarmax_gb300.synthetic)",
-                    "config": {"workload": WORKLOAD_BATCH.format(
-                        P=args.points, jk=" + 400 leave-one-bin-out jackknife NNLS per point" if args.jackknife else ""),
-                        "parallelism": f"replicas x{world}", "l2": "working set > L2 (no flush)",
-                        "setup_s": round(setup_s, 1)},
-                    "gpu_launches": int(launches), "clocks": clocks, "evals_per_step": evals_per_step,
-                    "logL_last": [float(v) for v in val.cpu().numpy()[:4]]}
-            if args.jackknife:
-                line["delta_chi2_last"] = [float(v) for v in r["jackknife"][:4]]
-            print(json.dumps(line))
-        if world > 1:
-            torch.distributed.destroy_process_group()
-        return
+    value = whole_job_rate(world, args.steps, ms)
     # --- per-stage device time of one evaluation (outside the timed region) ---------
     stages = stage_breakdown(lambda: step(0))
     # --- integrator kernel alone, for the roofline ----------------------------------
@@ -239,16 +204,7 @@ def run_ours(args, rank, world, local):
     # --- end to end through the public API with host buffers ------------------------------
     e2e = None
     if not args.skip_e2e:
-        host = {}
-        h2d = 0
-        for k, v in dict_data.items():
-            a = np.asarray(v)
-            if a.dtype.kind in "fi" and a.size > 8:
-                t = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
-                host[k] = t
-                h2d += t.numel() * t.element_size()
-            else:
-                host[k] = v
+        host, h2d = pinned_host_data(dict_data)
         if world > 1:
             torch.distributed.barrier()    # rank 0 has just run the FP64 comparison alone
         torch.cuda.synchronize()
@@ -281,6 +237,255 @@ def run_ours(args, rank, world, local):
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_batch(args, rank, world, local):
+    """Config 2, the metric's batched workload: one step = one batch of P parameter points
+    (jax.vmap(model_likelihood) of the reference's notebooks), each a full model
+    evaluation; value = evaluations per second.  Every point's orbits run in one
+    integrator launch fed by one work queue (autotuned launch shape and cost-ordered
+    queue), one projection launch bins all points, then the NNLS and maps of every point.
+    Reported beside it: per-stage times of one batch, the integrator's FP32 roofline, the
+    precision of point 0 against the plain FP64 kernels (same library and end to end),
+    the plain-FP64 rate of one evaluation, the end-to-end rate through
+    model_likelihood_batch with host buffers, and the 400-replicate jackknife of one point."""
+    import torch
+
+    from schwarmax_gb300 import _lib, engine, kernels, synthetic
+    from schwarmax_gb300.likelihood import grid_of, log_likelihoods, log_likelihoods_batch, log_mean_exp
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    cfg = synthetic.CONFIGS[2]
+    P = args.points
+    t0 = time.time()
+    dict_data, theta = synthetic.make_dataset(cfg, seed=args.seed)
+    setup_s = time.time() - t0
+    st = cfg.settings("mixed")
+    st.autotune = not args.no_autotune
+    dd = engine.DeviceData(dict_data, n_real=st.n_real)
+    nb = cfg.n_bins
+    nc = cfg.n_grid[0] * cfg.n_grid[1] * cfg.n_grid[2]
+    grid = grid_of(dict_data)
+    kw = dict(settings=st, nnls_maxiter=cfg.admm_iters)
+    points = synthetic.points_for(cfg, P, seed=args.seed + rank)
+
+    def batch(i, keep=False):
+        th = points.copy()
+        th[:, 10] = th[:, 10] + 0.002 * ((i % 5) - 2)          # M/L walk, MCMC-like
+        logl, r = log_likelihoods_batch(th, dd, nb, nc, keep=keep, max_points=args.points_per_launch, **kw)
+        m = torch.max(logl, dim=1, keepdim=True).values
+        return m[:, 0] + torch.log(torch.mean(torch.exp(logl - m), dim=1)), r
+
+    for i in range(args.warmup):
+        batch(i)
+    torch.cuda.synchronize()
+    # stage launches inside the timed region: CUDA events recorded on the launching stream
+    # (no synchronisation), and the integrator's buffers for its attempt count
+    names = ["initial_conditions", "integrate_batch", "project_bin_batch", "density_target", "nnls_admm",
+             "model_maps"]
+    events = {n: [] for n in names}
+    integ = []
+    orig = {n: getattr(kernels, n) for n in names}
+
+    def wrap(n):
+        def f(*a, **k):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            out = orig[n](*a, **k)
+            e1.record()
+            events[n].append((e0, e1))
+            # the integrator launch of the batch (a[7]: its IntegratorBuffers), not the queue-order probe's
+            if n == "integrate_batch" and a[7].slots == cfg.n_samples:
+                integ.append((e0, e1, a[7]))
+            return out
+        return f
+
+    sampler = clock_sampler(os.path.join(args.out, f"clocks_rank{rank}.csv")) if rank == 0 else None
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    launches0 = _lib.kernel_launches()
+    for n in names:
+        setattr(kernels, n, wrap(n))
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    try:
+        ev0.record()
+        for i in range(args.steps):
+            val, _ = batch(i)
+        ev1.record()
+        torch.cuda.synchronize()
+    finally:
+        for n in names:
+            setattr(kernels, n, orig[n])
+    if world > 1:
+        torch.distributed.barrier()
+    launches = _lib.kernel_launches() - launches0
+    ms = max_over_ranks(ev0.elapsed_time(ev1), dev)
+    if sampler:
+        sampler.terminate()
+    stages = {n: round(sum(a.elapsed_time(b) for a, b in events[n]) / args.steps, 3) for n in names}
+    stages["batch"] = round(ev0.elapsed_time(ev1) / args.steps, 3)
+    value = whole_job_rate(world, args.steps * P, ms)
+    # integrator roofline: arithmetic flops of the attempts / launch time, FP32 pipe
+    k_ms = sum(a.elapsed_time(b) for a, b, _ in integ) / max(len(integ), 1)
+    n_att = float(integ[-1][2].info[_lib.INFO_NATT].double().sum().item()) if integ else 0.0
+    flops = n_att * (3 * FLOPS_PER_FORCE + FLOPS_PER_STEP)
+    peaks = measured_peaks() or {}
+    clocks = clock_summary(os.path.join(args.out, f"clocks_rank{rank}.csv"), local) if rank == 0 else None
+    max_mhz = (clocks or {}).get("sm_max_mhz") or peaks.get("sm_max_mhz") or 2070.0
+    fp32_peak = 152 * 128 * 2 * max_mhz * 1e6 / 1e12
+    achieved = flops / (k_ms / 1e3) / 1e12 if k_ms > 0 else 0.0
+    roofline = {"kernel": "integrate_kernel<float, BATCH> (one launch per batch)", "bound": "fp32",
+                "achieved": round(achieved, 3), "peak": round(fp32_peak, 1), "unit": "TFLOP/s",
+                "frac": round(achieved / fp32_peak, 4),
+                "peak_source": "nominal FP32 FMA rate, 152 SMs x 128 lanes x 2 at the max SM clock "
+                               "(MEASURED_PEAKS.json holds no FP32 figure)",
+                "traffic": None, "ms_per_launch": round(k_ms, 3), "launches": len(integ), "attempts": n_att,
+                "flops_per_attempt": 3 * FLOPS_PER_FORCE + FLOPS_PER_STEP}
+    extra = {"stages_ms_per_batch": stages}
+    # --- end to end through the public API with host buffers (before the large workspaces below)
+    e2e = None
+    if not args.skip_e2e:
+        from schwarmax_gb300 import model_likelihood_batch
+        host, h2d = pinned_host_data(dict_data)
+        h2d += points.nbytes
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        t1 = time.time()
+        for i in range(args.e2e_steps):
+            th = points.copy()
+            th[:, 10] += 0.002 * ((i % 5) - 2)
+            model_likelihood_batch(th, host, nb, nc, settings=st, nnls_maxiter=cfg.admm_iters, cache=False)
+        torch.cuda.synchronize()
+        e2e_ms = max_over_ranks((time.time() - t1) * 1e3, dev)
+        e2e = {"value": whole_job_rate(world, args.e2e_steps * P, e2e_ms), "unit": UNIT,
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": 8 * P, "steps": args.e2e_steps}
+    if rank == 0:
+        torch.cuda.empty_cache()
+        # precision and the plain FP64 denominator on point 0 of the batch
+        if not args.skip_fp64:
+            th0 = points[0].copy()
+
+            def single(i):
+                th = th0.copy()
+                th[10] = th0[10] + 0.002 * ((i % 5) - 2)
+                logl, r = log_likelihoods(th, dd, nb, nc, **kw)
+                return log_mean_exp(logl), r
+            extra["precision"] = precision_and_fp64(cfg, dd, grid, nb, th0, st, single, value / world)
+            extra["precision"]["point"] = "point 0 of the batch"
+        if args.jackknife_points > 0:
+            # calculate_delta_chi2 (400 leave-one-bin-out replicates) on the libraries of the
+            # first points of the batch, timed after one untimed call on the same library
+            torch.cuda.empty_cache()
+            jp = min(args.jackknife_points, P)
+            _, r = batch(0, keep=True)
+            libs = {"libraries": [r["libraries"][0][:jp]]}
+            jackknife_batch(points[:1], libs, dd, nb, st, cfg.admm_iters)
+            torch.cuda.synchronize()
+            t1 = time.time()
+            dc = jackknife_batch(points[:jp], libs, dd, nb, st, cfg.admm_iters)
+            torch.cuda.synchronize()
+            extra["jackknife"] = {"points": jp, "replicates_per_point": nb,
+                                  "s_per_point": round((time.time() - t1) / jp, 3),
+                                  "delta_chi2": [float(v) for v in dc]}
+            del r, libs
+    cpu = None
+    if rank == 0 and world == 1 and not args.skip_cpu:
+        cpu = cpu_baseline(cfg, quick=True)
+    if rank == 0:
+        line = {"metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3), "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32 (orbits, binning) / bf16 split products + f64 (NNLS)",
+                "data": "synthetic (seeded; schwarmax_gb300.synthetic)",
+                "config": {"workload": WORKLOAD_BATCH.format(P=P, jk=""), "evals_per_step": P,
+                           "parallelism": f"replicas x{world}", "l2": "working set > L2 (no flush)",
+                           "setup_s": round(setup_s, 1), "autotune": st.autotune},
+                "gpu_launches": int(launches), "roofline": roofline, "e2e": e2e, "cpu_baseline": cpu,
+                "clocks": clocks, "logL_last": [float(v) for v in val.cpu().numpy()[:4]]}
+        line.update(extra)
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def critical_path(args):
+    """The integrator of one evaluation against the critical path of its longest orbits:
+    one launch over all orbits in queue order and in exact cost order (attempts of that
+    run, longest first), then the k longest orbits alone.  Prints one JSON object."""
+    import numpy as np
+    import torch
+
+    from schwarmax_gb300 import _lib, engine, kernels, synthetic
+    from schwarmax_gb300._lib import SMX_MODE_SAMPLED, SmxIntegrator
+    from schwarmax_gb300.likelihood import unpack_params
+    from schwarmax_gb300.potentials import potential_struct
+    cfg = synthetic.CONFIGS[args.config]
+    dict_data, theta = synthetic.make_dataset(cfg, seed=args.seed)
+    st = cfg.settings("mixed")
+    dd = engine.DeviceData(dict_data, n_real=st.n_real)
+    halo, bary = unpack_params(theta)
+    pot = potential_struct(bary, halo, st.bulge_mass)
+    pos, normals, uni = dd.cast(st.dtype, st.n_real)
+    ic = kernels.initial_conditions(pot, pos, normals, uni, st.n_real, st.n_periods, st.steps_per_period)
+    icfg = SmxIntegrator(mode=SMX_MODE_SAMPLED, store_all=0, n_attempts=st.n_attempts, n_samples=st.n_samples,
+                         max_attempts=st.max_attempts, atol=st.atol, rtol=st.rtol, dt_min=st.dt_min,
+                         dt_max=st.dt_max, omega=-float(bary["Omega_bar"]))
+
+    def timed(idx=None, order=None, reps=2):
+        w0, dt0, tt = ic["w0"], ic["dt_init"], ic["t_total"]
+        if idx is not None:
+            w0, dt0, tt = w0[:, idx].contiguous(), dt0[idx].contiguous(), tt[idx].contiguous()
+        bufs = kernels.IntegratorBuffers(w0.shape[1], st.n_samples, st.dtype, torch.device("cuda"))
+        icfg.order = 0 if order is None else order.data_ptr()
+        best = float("inf")
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record()
+            kernels.integrate(pot, icfg, w0, dt0, tt, bufs)
+            e1.record()
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        return best, bufs
+
+    out = {"workload": f"config {args.config}: {ic['w0'].shape[1]} orbits, {st.n_samples} samples"}
+    out["queue_order_ms"], bufs = timed()
+    att = bufs.info[_lib.INFO_NATT].double().cpu().numpy()
+    order = np.argsort(-att, kind="stable")
+    out["attempts"] = {"total": float(att.sum()), "mean": float(att.mean()), "median": float(np.median(att)),
+                       "p99": float(np.percentile(att, 99)), "max": float(att.max())}
+    w = att.reshape(-1, 32)
+    ws = att[order].reshape(-1, 32)
+    out["lane_use_queue_order"] = float(w.sum() / (32 * w.max(axis=1)).sum())
+    out["lane_use_cost_order"] = float(ws.sum() / (32 * ws.max(axis=1)).sum())
+    out["cost_order_ms"], _ = timed(order=torch.as_tensor(order.astype(np.int32), device="cuda"))
+    for k in (32, 152 * 32, 608 * 32):
+        if k < len(order):
+            out[f"longest_{k}_alone_ms"], _ = timed(idx=torch.as_tensor(order[:k].astype(np.int64), device="cuda"))
+    out["us_per_attempt_longest_alone"] = 1e3 * out["longest_32_alone_ms"] / float(att.max())
+    print(json.dumps(out))
+
+
+def pinned_host_data(dict_data):
+    """dict_data with its arrays in pinned host memory, and their bytes."""
+    import numpy as np
+    import torch
+    host, h2d = {}, 0
+    for k, v in dict_data.items():
+        a = np.asarray(v)
+        if a.dtype.kind in "fi" and a.size > 8:
+            t = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+            host[k] = t
+            h2d += t.numel() * t.element_size()
+        else:
+            host[k] = v
+    return host, h2d
 
 
 def jackknife_batch(thetas, r, dd, nb, st, maxiter):
@@ -452,7 +657,8 @@ def stage_breakdown(fn):
     import torch
 
     from schwarmax_gb300 import kernels
-    names = ["initial_conditions", "integrate", "project_bin", "density_target", "nnls_admm", "model_maps"]
+    names = ["initial_conditions", "integrate", "integrate_batch", "project_bin", "project_bin_batch",
+             "density_target", "nnls_admm", "model_maps"]
     events = {n: [] for n in names}
     orig = {n: getattr(kernels, n) for n in names}
 
@@ -606,9 +812,13 @@ def run_reference(args, rank, world):
 
 def adjoint_timing(dict_data, theta, cfg, st):
     """Config 3: the chi^2 gradient with respect to (alpha, beta, gamma, velocity
-    scale) on this evaluation's stored orbits (soft apertures, sigma 0.5 pixel),
-    timed after one warm-up gradient; one component checked by central
-    differences (step 1e-4 rad)."""
+    scale) on this evaluation's stored orbits (soft apertures, sigma 0.5 pixel), timed
+    after one warm-up gradient, and checked against central differences of all four
+    components at three points of the config's range: the viewing angles shifted by
+    -10, 0 and +10 degrees and the velocity scale 0.8, 1.0 and 1.2.  The difference
+    steps are 1e-5 rad and 1e-5 relative; a component whose free set (the orbits with
+    non-zero weight) differs between theta + h and theta - h is reported with that flag,
+    since chi^2 has a kink there and a central difference across it is not a derivative."""
     import numpy as np
     import torch
 
@@ -624,45 +834,79 @@ def adjoint_timing(dict_data, theta, cfg, st):
     c2, g = prob.chi2_and_grad(th, timings=tim)
     torch.cuda.synchronize()
     t_grad = time.time() - t0
-    fd = {}
-    for hstep in (1e-4, 1e-5):
-        e = np.array([hstep, 0.0, 0.0, 0.0])
-        fd[str(hstep)] = (prob.chi2(th + e) - prob.chi2(th - e)) / (2 * hstep)
-    g = g.cpu().numpy()
-    return {"workload": "config3: soft apertures (sigma 0.5 px) on the config-1 stored orbits, single data row, "
-                        "FP64 soft projection, ADMM + active-set KKT NNLS",
+
+    def free_set(t):
+        lib = prob.soft_library(t)
+        _, idx, _ = prob.solve(lib, prob.design(lib))
+        return set(idx.cpu().numpy().tolist())
+
+    checks = []
+    d10 = np.radians(10.0)
+    for shift, vs in ((-d10, 0.8), (0.0, 1.0), (d10, 1.2)):
+        t = th0.copy()
+        t[:3] += shift
+        t[3] = th0[3] * vs
+        c, gr = prob.chi2_and_grad(t)
+        gr = gr.cpu().numpy()
+        rows = []
+        for k in range(4):
+            h = 1e-5 if k < 3 else 1e-5 * t[3]
+            e = np.zeros(4)
+            e[k] = h
+            fd = (prob.chi2(t + e) - prob.chi2(t - e)) / (2 * h)
+            rows.append({"grad": float(gr[k]), "fd": float(fd),
+                         "rel_err": float(abs(gr[k] - fd) / max(abs(fd), 1e-300)),
+                         "free_set_changes": free_set(t + e) != free_set(t - e)})
+        checks.append({"angles_shift_deg": float(np.degrees(shift)), "vscale": float(t[3]), "chi2": c,
+                       "alpha": rows[0], "beta": rows[1], "gamma": rows[2], "vscale_grad": rows[3]})
+    return {"workload": "config3: soft apertures (sigma 0.5 px) on the stored orbits of one config-1 evaluation, "
+                        "single data row, FP64 soft projection, ADMM + active-set KKT NNLS; the gradient is that of "
+                        "the chi^2 of the converged KKT solution for the unperturbed data",
             "s_per_gradient": round(t_grad, 3), "stages_s": {k: (round(v, 3) if isinstance(v, float) else v)
                                                              for k, v in tim.items()},
-            "chi2": c2, "grad_alpha_beta_gamma_vscale": [float(v) for v in g],
-            "fd_alpha": fd, "fd_rel_err_alpha": {k: float(abs(g[0] - v) / max(abs(v), 1e-300)) for k, v in fd.items()}}
+            "chi2": c2, "grad_alpha_beta_gamma_vscale": [float(v) for v in g.cpu().numpy()],
+            "fd_checks": checks}
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="1", help="1 (the benchmark), 0, 4 or 'small' (profiler captures)")
+    ap.add_argument("--config", default="2",
+                    help="2 (the benchmark: batches of --points parameter points), 1 (one evaluation per step), "
+                         "0, 4 or 'small' (profiler captures)")
     ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=None, help="end-to-end steps (default 3; 1 batch for --config 2)")
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--points", type=int, default=64, help="parameter points per batch (--config 2)")
-    ap.add_argument("--autotune", action="store_true",
-                    help="--config 2: tuned integrator launch (blocks per SM, queue order; cached)")
-    ap.add_argument("--jackknife", action="store_true",
-                    help="--config 2: add the 400 leave-one-bin-out jackknife NNLS solves of every point")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="--config 2: natural integrator launch instead of the tuned one (blocks per SM, queue order)")
+    ap.add_argument("--points-per-launch", type=int, default=None,
+                    help="--config 2: parameter points per integrator launch (default: engine.MAX_POINTS_PER_LAUNCH)")
+    ap.add_argument("--critical-path", action="store_true",
+                    help="--config 1: time the integrator launch in queue order and in cost order, and the longest "
+                         "orbits alone (32, 4,864 and 19,456 of them), and print them with the attempt statistics")
+    ap.add_argument("--jackknife-points", type=int, default=1,
+                    help="--config 2: points of the batch whose 400-replicate leave-one-bin-out jackknife is timed")
     ap.add_argument("--adjoint", action="store_true",
                     help="also time the chi^2 gradient of the differentiable projection + NNLS on this library")
     ap.add_argument("--out", default=os.path.join(ROOT, "bench_out"), help="folder for the clock samples")
     args = ap.parse_args()
     args.config = int(args.config) if args.config.isdigit() else args.config
     os.makedirs(args.out, exist_ok=True)
+    if args.e2e_steps is None:
+        args.e2e_steps = 1 if args.config == 2 else 3
     rank, world, local = dist_env()
     if args.impl == "reference":
         run_reference(args, rank, world)
+    elif args.config == 2:
+        run_batch(args, rank, world, local)
+    elif args.critical_path:
+        critical_path(args)
     else:
         run_ours(args, rank, world, local)
 

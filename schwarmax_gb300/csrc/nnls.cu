@@ -104,7 +104,7 @@ static SplitShapes split_shapes(const smx_nnls_problem *p) {
     sh.Ut = split::make_operand(n, m, split::MT, 4);    // orbits over rows of U
     sh.Xg = split::make_operand(m, m, split::MT, 5);
     sh.Ds = split::make_operand(B, n, vt, 5);
-    sh.Es = split::make_operand(B, m, 64, 5);   // G^-1 E: 64-wide tiles, five exact levels
+    sh.Es = split::make_operand(B, m, vt, 5);   // jackknife: inputs of the Neumann terms
     sh.Fs = split::make_operand(B, m, vt, 5);
     sh.G7 = split::make_operand(m, m, split::MT, 7);
     sh.X7 = split::make_operand(m, m, 96, 7);
@@ -300,8 +300,12 @@ enum { COL_INIT = 0, COL_RESID = 1, COL_PLAIN = 2, COL_UPDATE = 3 };
 constexpr int kNsMaxSteps = 5;   // Newton-Schulz steps at most (a seed residual of 0.2 needs 4)
 
 constexpr int VS = 5;          // slices of the vector operands: 39 bits below each column's largest magnitude
-// slice pairs (s, t) of the skinny products U D, H^T E (jackknife: U^T F) with s + t <= kSkinnyLevels
-constexpr int kSkinnyLevels = 7;
+// Slice pairs (s, t) of the skinny products U D and H^T E with s + t <= kSkinnyLevels.
+// The pairs left out (s + t >= 6) weigh 2^-32 of max|A| max|B| per term, the size of
+// the 31-bit slicing of U and H; at 16,384 orbits x 6,608 rows x 100 right-hand sides
+// levels 7, 6 and 5 gave a largest bootstrap delta chi^2 against FP64 of 1.3e-3, 1.3e-3
+// and 1.5e-3 on the same library; at level 5 the products form 10 slice pairs instead of 17.
+constexpr int kSkinnyLevels = 5;
 constexpr int COL_CHUNK = 1024;   // k per CTA of the column kernels
 
 struct ColArgs {
@@ -325,6 +329,9 @@ struct ColArgs {
     int64_t k_tiles, slice_elems;
     int tile_rows;
     int t_shift;             // units of the product's T: 2^-t_shift
+    // COL_UPDATE of the jackknife (optional): w -= sum_q cvec[j, q] hrows[j, q, :]
+    const double *hrows, *cvec;
+    int max_drop;
 };
 
 // Phase 1 of a column step, grid (K / COL_CHUNK, n_rhs): forms the new column values
@@ -386,7 +393,10 @@ __global__ void __launch_bounds__(256) column_values_kernel(const ColArgs a) {
             a.R[idx] = 0.0f;
             if (MODE == COL_UPDATE) {
                 const double z = y[q], u = uu[q];
-                const double w = x[q] + pv;
+                double w = x[q] + pv;
+                if (a.hrows)
+                    for (int t = 0; t < a.max_drop; ++t)
+                        w -= a.cvec[j * a.max_drop + t] * a.hrows[(j * a.max_drop + t) * K + k];
                 const double wh = 1.6 * w - 0.6 * z;
                 double zn = wh + u;
                 zn = zn > 0.0 ? zn : 0.0;
@@ -507,16 +517,16 @@ __global__ void ns_verdict_kernel(const int *flag, int *dinfo) {
 // residual R = I - G X of a Newton-Schulz step.  G and X are dominated by their
 // diagonals, so G X = D_G X + O_G D_X + O_G O_X with D the diagonals and O the
 // rest: the first two terms are formed here in double, only O_G O_X comes from
-// the split product (four exact levels, T in units of 2^-24).  rss receives
-// sum R_ij^2 (||R||_F^2, a bound on ||R||_2^2).
+// the split product (T in units of 2^-t_shift).  rss receives sum R_ij^2
+// (||R||_F^2, a bound on ||R||_2^2).
 __global__ void ns_residual_kernel(unsigned long long *T, float *Racc, const int32_t *eG, const int32_t *eX,
                                    const double *G, const double *X, double *Rd, int64_t m, double *rss,
-                                   const int *skip) {
+                                   const int *skip, int t_shift) {
     if (*skip) return;
     double acc = 0;
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < m * m; k += (int64_t)gridDim.x * blockDim.x) {
         const int64_t r = k % m, col = k / m;
-        double gx = ldexp((double)(long long)T[k] * 0x1p-24 + (double)Racc[k], eG[r] + eX[col] - 14);
+        double gx = product_of((long long)T[k], Racc[k], eG[r], eX[col], t_shift);
         gx += G[r + m * r] * X[k];
         if (r != col) gx += G[k] * X[col + m * col];
         const double v = (r == col ? 1.0 : 0.0) - gx;
@@ -532,11 +542,11 @@ __global__ void ns_residual_kernel(unsigned long long *T, float *Racc, const int
 
 // X <- X + X R
 __global__ void ns_update_kernel(unsigned long long *T, float *Racc, const int32_t *eX, const int32_t *eR, double *X,
-                                 int64_t m, const int *skip) {
+                                 int64_t m, const int *skip, int t_shift) {
     if (*skip) return;
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < m * m; k += (int64_t)gridDim.x * blockDim.x) {
         const int64_t r = k % m, col = k / m;
-        X[k] += product_value(T, Racc, k, eX[r], eR[col]);
+        X[k] += product_value(T, Racc, k, eX[r], eR[col], t_shift);
         T[k] = 0ull;
         Racc[k] = 0.0f;
     }
@@ -571,6 +581,8 @@ __global__ void h_combine_kernel(unsigned long long *T, float *R, const int32_t 
     }
 }
 
+__global__ void rownorm_kernel(const double *__restrict__ U, int64_t m, int64_t n, double *out);
+
 // The set-up of the mixed path shared by the bootstrap and jackknife solvers: U in
 // double, ||U||_F^2 and the ADMM coefficient, U sliced both ways, G = U U^T + c I
 // from the slices, G^-1 by a float seed and Newton-Schulz steps, and G^-1 split into
@@ -586,7 +598,7 @@ struct MixedState {
 template <typename TL>
 static int mixed_setup(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map, const double *row_scale,
                        unsigned char *ws, const Layout &L, Handles *h, cudaStream_t s, MixedState &S,
-                       bool make_h = false) {
+                       bool make_h = false, double *rownorm = nullptr) {
     const int64_t m = p->m, n = p->n;
     const double lam = p->lambda_reg;
     double *G = (double *)(ws + L.G);
@@ -603,6 +615,11 @@ static int mixed_setup(const smx_nnls_problem *p, const TL *lib, const int32_t *
     count_launch();
     admm_coef_kernel<<<1, 1, 0, s>>>(frob, lam, (double)n, frob + 1);
     count_launch();
+    if (rownorm) {   // ||U_r||^2 of every design row, before U is replaced by H
+        SMX_TRY_CUDA(cudaMemsetAsync(rownorm, 0, m * sizeof(double), s));
+        rownorm_kernel<<<dim3((unsigned)((m + 255) / 256), 64), 256, 0, s>>>(U, m, n, rownorm);
+        count_launch();
+    }
     SplitShapes sh = split_shapes(p);
     sh.Ua.slices = (__nv_bfloat16 *)(ws + L.Ua);
     sh.Ua.expo = (int32_t *)(ws + L.Ua_e);
@@ -668,16 +685,24 @@ static int mixed_setup(const smx_nnls_problem *p, const TL *lib, const int32_t *
     count_launch();
     const int *skip = nsf + 3;
     for (int step = 0; step < kNsMaxSteps; ++step) {
+        // The first step starts from the float seed (||I - G X0|| ~ 2e-3): its output is
+        // only as good as ||R0||^2 ~ 4e-6, so its products keep 3 slices (23 bits, errors
+        // ~1e-7 after the cond(G) ~ 2e3 amplification of the update); later steps use 7
+        // (residual) and 5 (update).  A poorer seed costs one more full step, not accuracy.
+        split::Operand g = sh.G7, x = sh.X7, xr = sh.X5, rr = sh.R5;
+        if (step == 0) g.S = x.S = xr.S = rr.S = 3;
         if ((st = split::slice_rows<double>(Xd, m, 1, sh.X7, rowmax, s, true, skip))) return st;   // O_X columns over k
-        if ((st = split::gemm(sh.G7, sh.X7, acc, false, derr, s, 0, skip))) return st;
+        if ((st = split::gemm(g, x, acc, false, derr, s, 0, skip))) return st;
         SMX_TRY_CUDA(cudaMemsetAsync(rss, 0, sizeof(double), s));
-        ns_residual_kernel<<<grid1d(m * m), 256, 0, s>>>(Tacc, Racc, sh.G7.expo, sh.X7.expo, G, Xd, Rd, m, rss, skip);
+        ns_residual_kernel<<<grid1d(m * m), 256, 0, s>>>(Tacc, Racc, sh.G7.expo, sh.X7.expo, G, Xd, Rd, m, rss, skip,
+                                                         8 * (split::exact_levels(g, x) - 1));
         ns_gate_kernel<<<1, 1, 0, s>>>(rss, 1e-10, nsf);
         count_launch(2);
         if ((st = split::slice_rows<double>(Xd, 1, m, sh.X5, rowmax, s, false, skip))) return st;   // X rows over k
         if ((st = split::slice_rows<double>(Rd, m, 1, sh.R5, rowmax, s, false, skip))) return st;   // R columns over k
-        if ((st = split::gemm(sh.X5, sh.R5, acc, false, derr, s, 0, skip))) return st;
-        ns_update_kernel<<<grid1d(m * m), 256, 0, s>>>(Tacc, Racc, sh.X5.expo, sh.R5.expo, Xd, m, skip);
+        if ((st = split::gemm(xr, rr, acc, false, derr, s, 0, skip))) return st;
+        ns_update_kernel<<<grid1d(m * m), 256, 0, s>>>(Tacc, Racc, sh.X5.expo, sh.R5.expo, Xd, m, skip,
+                                                       8 * (split::exact_levels(xr, rr) - 1));
         ns_skip_kernel<<<1, 1, 0, s>>>(nsf);
         count_launch(2);
     }
@@ -772,6 +797,7 @@ static int run(const smx_nnls_problem *p, const TL *lib, const int32_t *row_map,
         auto col = [&](int mode, int64_t K, const int32_t *eA, const int32_t *eB, split::Operand &out,
                        int t_shift) -> int {
             ColArgs a;
+            memset(&a, 0, sizeof(a));
             a.K = K;
             a.n_rhs = B;
             a.T = Tacc;
@@ -943,8 +969,10 @@ __global__ void jk_setup_kernel(const int32_t *__restrict__ drop, int max_drop, 
 }
 
 // E = Y - U D with the replicate's dropped rows set to 0; Y is the shared data row.
-// Grid (K / COL_CHUNK, replicates).  T, R of the product are cleared.
-__global__ void __launch_bounds__(256) jk_resid_kernel(const ColArgs a, const int32_t *__restrict__ row_group) {
+// W = E starts the sum of the Neumann terms.  Grid (K / COL_CHUNK, replicates).
+// T, R of the product are cleared.
+__global__ void __launch_bounds__(256) jk_resid_kernel(const ColArgs a, const int32_t *__restrict__ row_group,
+                                                       double *W) {
     constexpr int PER = COL_CHUNK / 256;
     const int64_t j = blockIdx.y, K = a.K;
     const int eb = a.eB[j];
@@ -959,6 +987,7 @@ __global__ void __launch_bounds__(256) jk_resid_kernel(const ColArgs a, const in
         a.R[idx] = 0.0f;
         const double v = row_group[k] == (int32_t)j ? 0.0 : a.Y[k] - pv;
         a.E[idx] = v;
+        W[idx] = v;
         mx = fmax(mx, fabs(v));
     }
 #pragma unroll
@@ -998,12 +1027,12 @@ __global__ void jk_dvals_kernel(const unsigned long long *__restrict__ T, const 
 }
 
 // One Neumann term for every replicate, grid (K / COL_CHUNK, replicates):
-//   P = g V + O V - X_{:,d} c  (P = 0 on d),  F (+)= P,  V = delta_j P,
-// and the column maxima of the operand sliced next (V, or F after the last term).
+//   P = g V + O V - X_{:,d} c = S V  (P = 0 on d),  V = delta_j P,  W += V,
+// and the column maxima of the operand sliced next (V, or W after the last term).
 __global__ void __launch_bounds__(256) jk_apply_kernel(const ColArgs a, const int32_t *__restrict__ row_group,
                                                        const int32_t *__restrict__ drop, int max_drop,
                                                        const double *__restrict__ O, const double *__restrict__ cbuf,
-                                                       const double *__restrict__ mu, double *F, int first, int last) {
+                                                       const double *__restrict__ mu, double *F, int last) {
     constexpr int PER = COL_CHUNK / 256;
     const int64_t j = blockIdx.y, K = a.K;
     const int eb = a.eB[j];
@@ -1038,9 +1067,9 @@ __global__ void __launch_bounds__(256) jk_apply_kernel(const ColArgs a, const in
             P = a.g[k] * a.E[idx] + pv;
             for (int t = 0; t < sz; ++t) P -= O[k + K * (int64_t)dr[t]] * cc[t];
         }
-        const double f = first ? P : F[idx] + P;
-        F[idx] = f;
         const double v = muj * P;
+        const double f = F[idx] + v;
+        F[idx] = f;
         a.E[idx] = v;
         mx = fmax(mx, fabs(last ? f : v));
     }
@@ -1056,11 +1085,82 @@ __global__ void __launch_bounds__(256) jk_apply_kernel(const ColArgs a, const in
     }
 }
 
+// Rows d_j of H = G^-1 U for every replicate, compacted: Hr[(j max_drop + q) n + i] =
+// H[d + m i] for the q-th valid entry d of drop[j], 0 beyond the replicate's drops.
+__global__ void jk_hrows_kernel(const double *__restrict__ H, int64_t m, int64_t n, const int32_t *__restrict__ drop,
+                                int max_drop, int64_t G, double *Hr) {
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < G * max_drop * n;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t jq = idx / n, i = idx % n, j = jq / max_drop;
+        const int q = (int)(jq % max_drop);
+        int c = 0;
+        int32_t d = -1;
+        for (int t = 0; t < max_drop; ++t) {
+            const int32_t r = drop[j * max_drop + t];
+            if (r >= 0) {
+                if (c == q) {
+                    d = r;
+                    break;
+                }
+                ++c;
+            }
+        }
+        Hr[idx] = d >= 0 ? H[d + m * i] : 0.0;
+    }
+}
+
+// c_j = (X_dd)^-1 (X W_j)_d exactly in double, one CTA per replicate: W_j vanishes
+// on d, so (X W)_d = O_{d,:} W (column d of the symmetric O); cbuf[j max_drop + q]
+// for the replicate's q-th drop, 0 beyond them.
+__global__ void __launch_bounds__(256) jk_xdots_kernel(const double *__restrict__ O, const double *__restrict__ W,
+                                                       int64_t m, const int32_t *__restrict__ drop, int max_drop,
+                                                       const double *__restrict__ Zinv, double *cbuf) {
+    const int64_t j = blockIdx.x;
+    __shared__ double dots[JK_MAX_DROP];
+    __shared__ double red[8];
+    __shared__ int32_t dr[JK_MAX_DROP];
+    __shared__ int sz;
+    if (threadIdx.x == 0) {
+        int q = 0;
+        for (int t = 0; t < max_drop; ++t) {
+            const int32_t r = drop[j * max_drop + t];
+            if (r >= 0) dr[q++] = r;
+        }
+        sz = q;
+    }
+    __syncthreads();
+    const double *w = W + m * j;
+    for (int q = 0; q < sz; ++q) {
+        const double *col = O + m * (int64_t)dr[q];
+        double acc = 0;
+        for (int64_t k = threadIdx.x; k < m; k += blockDim.x) acc += col[k] * w[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = 0;
+            for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += red[i];
+            dots[q] = t;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x < max_drop) {
+        const int q = threadIdx.x;
+        double c = 0;
+        if (q < sz) {
+            const double *Z = Zinv + j * (int64_t)max_drop * max_drop;
+            for (int b = 0; b < sz; ++b) c += Z[q * max_drop + b] * dots[b];
+        }
+        cbuf[j * max_drop + q] = c;
+    }
+}
+
 struct JkLayout {
-    size_t rownorm, kcoef, mu, Zinv, cbuf, rowgrp, qmax, flag, dummy, total;
+    size_t rownorm, kcoef, mu, Zinv, cbuf, rowgrp, qmax, flag, dummy, hrows, total;
 };
 
-static JkLayout jk_layout(size_t base, int64_t m, int64_t G, int max_drop) {
+static JkLayout jk_layout(size_t base, int64_t m, int64_t n, int64_t G, int max_drop) {
     JkLayout J;
     size_t off = base;
     auto take = [&](size_t bytes) { size_t o = off; off = align256(off + bytes); return o; };
@@ -1073,6 +1173,7 @@ static JkLayout jk_layout(size_t base, int64_t m, int64_t G, int max_drop) {
     J.qmax = take(sizeof(unsigned long long));
     J.flag = take(4 * sizeof(int));
     J.dummy = take(G * sizeof(unsigned long long));
+    J.hrows = take((size_t)G * max_drop * n * sizeof(double));
     J.total = off;
     return J;
 }
@@ -1090,24 +1191,25 @@ static int run_jackknife(const smx_nnls_problem *p, const TL *lib, const int32_t
     SMX_TRY_CUDA(cudaMemsetAsync(jflag, 0, 4 * sizeof(int), s));
     MixedState S;
     int st;
-    if ((st = mixed_setup<TL>(p, lib, row_map, row_scale, ws, L, h, s, S))) return st;
-    SplitShapes &sh = S.sh;
     double *rownorm = (double *)(ws + J.rownorm), *kcoef = (double *)(ws + J.kcoef), *mu = (double *)(ws + J.mu);
+    // the set-up with H = G^-1 U (U's row norms are taken before U is replaced by H)
+    if ((st = mixed_setup<TL>(p, lib, row_map, row_scale, ws, L, h, s, S, true, rownorm))) return st;
+    SplitShapes &sh = S.sh;
     double *Zinv = (double *)(ws + J.Zinv), *cbuf = (double *)(ws + J.cbuf);
     int32_t *rowgrp = (int32_t *)(ws + J.rowgrp);
     unsigned long long *qmax = (unsigned long long *)(ws + J.qmax);
-    SMX_TRY_CUDA(cudaMemsetAsync(rownorm, 0, m * sizeof(double), s));
+    double *Hr = (double *)(ws + J.hrows);
     SMX_TRY_CUDA(cudaMemsetAsync(rowgrp, 0xff, m * sizeof(int32_t), s));
     SMX_TRY_CUDA(cudaMemsetAsync(qmax, 0, sizeof(unsigned long long), s));
     jk_rowgroup_kernel<<<grid1d(B * max_drop), 256, 0, s>>>(drop, max_drop, B, m, rowgrp, jflag);
-    count_launch();
-    rownorm_kernel<<<dim3((unsigned)((m + 255) / 256), 64), 256, 0, s>>>(S.U, m, n, rownorm);
     count_launch();
     jk_setup_kernel<<<(unsigned)((B + 63) / 64), 64, 0, s>>>(drop, max_drop, B, rownorm, frob, p->lambda_reg,
                                                              (double)n, S.Xd, S.gdiag, m, kcoef, mu, Zinv, qmax,
                                                              jflag + 1);
     count_launch();
-    // the number of Neumann terms follows the largest delta_j / c (one read-back)
+    jk_hrows_kernel<<<grid1d(B * max_drop * n), 256, 0, s>>>(S.U, m, n, drop, max_drop, B, Hr);
+    count_launch();
+    // the number of Neumann terms and their slices follow the largest delta_j / c (one read-back)
     unsigned long long hq = 0;
     int hflag[4] = {0, 0, 0, 0};
     SMX_TRY_CUDA(cudaMemcpyAsync(&hq, qmax, sizeof(hq), cudaMemcpyDeviceToHost, s));
@@ -1120,11 +1222,19 @@ static int run_jackknife(const smx_nnls_problem *p, const TL *lib, const int32_t
     memcpy(&qv, &hq, sizeof(qv));
     if (!(qv < 0.5))
         return set_error(SMX_ERR_UNSUPPORTED, "smx_nnls_jackknife: a group carries %.3g of ||U||_F^2 (at most 0.5)", qv);
+    // Replicate j's update is w = D + U^T S_j W_j with W_j = sum_t (delta_j S_j)^t E_j,
+    // S_j = (G_KK)^-1 (Schur complement of the dropped rows of X = G^-1).  Since W_j
+    // vanishes on d_j, U^T S_j W_j = H^T W_j - H_{d,:}^T (X_dd)^-1 (X W_j)_d: one
+    // product with H^T for all replicates plus a rank-|d_j| correction formed exactly.
+    // Term t of W is about q^t of term 0 (q = max delta_j / c): terms follow while
+    // q^t > 1e-12 (the 2^-39 slicing of the vectors), and the product of term t keeps
+    // the slices that carry its 40 - t log2(1/q) significant bits.
     int terms = 1;
-    for (double t = qv; t > 1e-15 && terms < 64; t *= qv) ++terms;
+    for (double t = qv; t > 1e-12 && terms < 64; t *= qv) ++terms;
+    const double lq = qv > 0 ? -log2(qv) : 64.0;
     double *Z = (double *)(ws + L.Z), *Uu = (double *)(ws + L.Uu), *D = (double *)(ws + L.D);
-    double *Ebuf = (double *)(ws + L.Ebuf), *Fbuf = (double *)(ws + L.Fbuf);
-    unsigned long long *cmD = (unsigned long long *)(ws + L.colmax), *cmE = cmD + B, *cmF = cmE + B;
+    double *Ebuf = (double *)(ws + L.Ebuf), *Wbuf = (double *)(ws + L.Fbuf);
+    unsigned long long *cmD = (unsigned long long *)(ws + L.colmax), *cmE = cmD + B, *cmW = cmE + B;
     unsigned long long *dummy = (unsigned long long *)(ws + J.dummy);
     SMX_TRY_CUDA(cudaMemsetAsync(cmD, 0, 3 * B * sizeof(unsigned long long), s));
     auto args = [&](int64_t K, const int32_t *eA, const int32_t *eB, split::Operand &out, int t_shift, double *V,
@@ -1164,8 +1274,7 @@ static int run_jackknife(const smx_nnls_problem *p, const TL *lib, const int32_t
     };
     split::Acc acc_m{S.Tacc, S.Racc, m}, acc_n{S.Tacc, S.Racc, n};
     const int sh_ud = 8 * (split::exact_levels(sh.Ua, sh.Ds) - 1);
-    const int sh_ge = 8 * (split::exact_levels(sh.Xg, sh.Es) - 1);
-    const int sh_uf = 8 * (split::exact_levels(sh.Ut, sh.Fs) - 1);
+    const int sh_hw = 8 * (split::exact_levels(sh.Ut, sh.Fs) - 1);
     const dim3 gm((unsigned)((m + COL_CHUNK - 1) / COL_CHUNK), (unsigned)B);
     const dim3 gn((unsigned)((n + COL_CHUNK - 1) / COL_CHUNK), (unsigned)B);
     {   // z = w_init, u = 0, D = k_j w_init, sliced
@@ -1178,30 +1287,42 @@ static int run_jackknife(const smx_nnls_problem *p, const TL *lib, const int32_t
         if ((st = split::gemm(sh.Ua, sh.Ds, acc_m, false, S.derr, s, kSkinnyLevels))) return st;   // U D
         SMX_TRY_CUDA(cudaMemsetAsync(cmE, 0, B * sizeof(unsigned long long), s));
         {
-            ColArgs a = args(m, sh.Ua.expo, sh.Ds.expo, sh.Es, sh_ud, Ebuf, cmE);
-            jk_resid_kernel<<<gm, 256, 0, s>>>(a, rowgrp);                             // E = mask(Y - U D)
-            count_launch();
-            slices(a, sh.Es);
-        }
-        for (int t = 0; t < terms; ++t) {
-            const bool last = t == terms - 1;
-            if ((st = split::gemm(sh.Xg, sh.Es, acc_m, false, S.derr, s))) return st;   // O V
-            jk_dvals_kernel<<<(unsigned)((B + 127) / 128), 128, 0, s>>>(S.Tacc, S.Racc, sh.Xg.expo, sh.Es.expo, sh_ge,
-                                                                        drop, max_drop, B, m, Zinv, cbuf);
-            count_launch();
-            unsigned long long *cm = last ? cmF : cmE;
-            SMX_TRY_CUDA(cudaMemsetAsync(cm, 0, B * sizeof(unsigned long long), s));
-            split::Operand &out = last ? sh.Fs : sh.Es;
-            ColArgs a = args(m, sh.Xg.expo, sh.Es.expo, out, sh_ge, last ? Fbuf : Ebuf, cm);
-            jk_apply_kernel<<<gm, 256, 0, s>>>(a, rowgrp, drop, max_drop, S.Xd, cbuf, mu, Fbuf, t == 0 ? 1 : 0,
-                                               last ? 1 : 0);
+            // E = mask(Y - U D) = W (first term); sliced as the next product's input
+            split::Operand &out = terms > 1 ? sh.Es : sh.Fs;
+            ColArgs a = args(m, sh.Ua.expo, sh.Ds.expo, out, sh_ud, Ebuf, cmE);
+            jk_resid_kernel<<<gm, 256, 0, s>>>(a, rowgrp, Wbuf);
             count_launch();
             slices(a, out);
         }
-        if ((st = split::gemm(sh.Ut, sh.Fs, acc_n, false, S.derr, s, kSkinnyLevels))) return st;   // U^T F
+        for (int t = 1; t < terms; ++t) {
+            const bool last = t == terms - 1;
+            int sl = (int)ceil((40.0 - t * lq + 1.0) / 8.0);
+            sl = sl < 2 ? 2 : (sl > 5 ? 5 : sl);
+            split::Operand Ot = sh.Xg, Vt = sh.Es;
+            Ot.S = sl;
+            Vt.S = sl;
+            const int sh_ov = 8 * (split::exact_levels(Ot, Vt) - 1);
+            if ((st = split::gemm(Ot, Vt, acc_m, false, S.derr, s))) return st;   // O V
+            jk_dvals_kernel<<<(unsigned)((B + 127) / 128), 128, 0, s>>>(S.Tacc, S.Racc, sh.Xg.expo, sh.Es.expo, sh_ov,
+                                                                        drop, max_drop, B, m, Zinv, cbuf);
+            count_launch();
+            unsigned long long *cm = last ? cmW : cmE;
+            SMX_TRY_CUDA(cudaMemsetAsync(cm, 0, B * sizeof(unsigned long long), s));
+            split::Operand &out = last ? sh.Fs : sh.Es;
+            ColArgs a = args(m, sh.Xg.expo, sh.Es.expo, out, sh_ov, last ? Wbuf : Ebuf, cm);
+            jk_apply_kernel<<<gm, 256, 0, s>>>(a, rowgrp, drop, max_drop, S.Xd, cbuf, mu, Wbuf, last ? 1 : 0);
+            count_launch();
+            slices(a, out);
+        }
+        if ((st = split::gemm(sh.Ut, sh.Fs, acc_n, false, S.derr, s, kSkinnyLevels))) return st;   // H^T W
+        jk_xdots_kernel<<<(unsigned)B, 256, 0, s>>>(S.Xd, Wbuf, m, drop, max_drop, Zinv, cbuf);        // c_j
+        count_launch();
         SMX_TRY_CUDA(cudaMemsetAsync(cmD, 0, B * sizeof(unsigned long long), s));
         {
-            ColArgs a = args(n, sh.Ut.expo, sh.Fs.expo, sh.Ds, sh_uf, D, cmD);
+            ColArgs a = args(n, sh.Ut.expo, sh.Fs.expo, sh.Ds, sh_hw, D, cmD);
+            a.hrows = Hr;
+            a.cvec = cbuf;
+            a.max_drop = max_drop;
             column_values_kernel<COL_UPDATE><<<gn, 256, 0, s>>>(a);                     // ADMM update, D
             count_launch();
             slices(a, sh.Ds);
@@ -1278,8 +1399,8 @@ extern "C" int smx_nnls_jackknife_workspace_size(const smx_nnls_problem *p, int 
     smx_nnls_problem q = *p;
     q.mode = SMX_NNLS_MIXED;
     Layout L;
-    if ((st = layout(&q, &L, h->solver, false))) return st;
-    *bytes = jk_layout(L.total, p->m, p->n_rhs, max_drop).total;
+    if ((st = layout(&q, &L, h->solver))) return st;
+    *bytes = jk_layout(L.total, p->m, p->n, p->n_rhs, max_drop).total;
     return SMX_OK;
 }
 
@@ -1302,8 +1423,8 @@ extern "C" int smx_nnls_jackknife(const smx_nnls_problem *p, const void *library
     int st = get_handles(s, &h);
     if (st) return st;
     Layout L;
-    if ((st = layout(p, &L, h->solver, false))) return st;
-    const JkLayout J = jk_layout(L.total, p->m, p->n_rhs, max_drop);
+    if ((st = layout(p, &L, h->solver))) return st;
+    const JkLayout J = jk_layout(L.total, p->m, p->n, p->n_rhs, max_drop);
     if (workspace_bytes < J.total)
         return set_error(SMX_ERR_WORKSPACE, "smx_nnls_jackknife: workspace %zu < %zu bytes", workspace_bytes, J.total);
     unsigned char *ws = (unsigned char *)workspace;

@@ -108,9 +108,52 @@ __global__ void sample_cells_kernel(GeoT<T> G, const T *__restrict__ pts, int64_
     }
 }
 
+// round(x 2^56) of a float with |x| < 2^6 as an int64, round half to even (the value of
+// __float2ll_rn(x * 2^56)), from the bits of x: integer operations only, as the int64
+// conversion instruction runs on the FP64 pipe, 1/64 of the FP32 rate on this GPU.
+__device__ __forceinline__ long long fixed56(float x) {
+    const unsigned u = __float_as_uint(x);
+    const int e = (int)((u >> 23) & 0xFF);
+    if (e == 0) return 0;                              // zero, subnormals (|x 2^56| < 2^-69)
+    const long long m = (long long)((u & 0x7FFFFFu) | 0x800000u);
+    const int sh = e - 94;                             // x 2^56 = m 2^(e - 150 + 56)
+    long long v;
+    if (sh > 39) {
+        return (long long)0x8000000000000000ull;       // |x| >= 2^7 (or not finite): out of range
+    } else if (sh >= 0) {
+        v = m << sh;
+    } else if (sh < -24) {
+        v = 0;
+    } else {
+        const int r = -sh;
+        const long long q = m >> r, rem = m & ((1LL << r) - 1), half = 1LL << (r - 1);
+        v = q + ((rem > half || (rem == half && (q & 1))) ? 1 : 0);
+    }
+    return (u >> 31) ? -v : v;
+}
+
+// A finite double rounded to the nearest float (ties to even), from its bits; values
+// below the normal float range become a signed zero.  Integer operations only (the
+// conversion instruction, like all FP64 work, runs at 1/64 of the FP32 rate here).
+__device__ __forceinline__ float float_of(double d) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    const unsigned sign = (unsigned)(b >> 63) << 31;
+    int e = (int)((b >> 52) & 0x7FF) - 1023 + 127;
+    if (e <= 0) return __uint_as_float(sign);
+    unsigned long long mant = (b & ((1ull << 52) - 1)) >> 29;
+    const unsigned long long rem = b & ((1ull << 29) - 1), half = 1ull << 28;
+    mant += (rem > half || (rem == half && (mant & 1))) ? 1 : 0;
+    if (mant >> 23) {
+        mant = 0;
+        ++e;
+    }
+    if (e >= 255) return __uint_as_float(sign | 0x7F800000u);
+    return __uint_as_float(sign | ((unsigned)e << 23) | (unsigned)mant);
+}
+
 // Adds x rounded to a multiple of 2^-56 (|x| < 2^6) to an int64 fixed-point sum.
 __device__ __forceinline__ void fixed_add(unsigned long long *a, float x) {
-    atomicAdd(a, (unsigned long long)__float2ll_rn(x * 0x1p56f));
+    atomicAdd(a, (unsigned long long)fixed56(x));
 }
 __device__ __forceinline__ void fixed_add(unsigned long long *a, double x) {
     atomicAdd(a, (unsigned long long)__double2ll_rn(x * 0x1p56));
@@ -195,8 +238,15 @@ __global__ void __launch_bounds__(256) project_bin_kernel(GeoT<T> G, const T *__
                 project_image(G, rot, x, y, z, vx, vy, vz, bin_mapping, cell, b, vl);
                 if (cell < G.n_cells) fixed_add(&acc[cell], w);
                 if (b < 0 || b >= nb) continue;
-                const T s_b = T(__ldg(&sg[b]));
-                const T yv = (vl * kms - T(__ldg(&v0g[b]))) / s_b;
+                T s_b, v0_b;
+                if constexpr (sizeof(T) == 4) {
+                    s_b = float_of(__ldg(&sg[b]));
+                    v0_b = float_of(__ldg(&v0g[b]));
+                } else {
+                    s_b = __ldg(&sg[b]);
+                    v0_b = __ldg(&v0g[b]);
+                }
+                const T yv = (vl * kms - v0_b) / s_b;
                 // g without its 1/s_b (applied when the row is written)
                 const T gw = w * isq2pi * M<T>::exp(T(-0.5) * yv * yv);
                 const T H1 = sq2 * yv;
@@ -214,11 +264,23 @@ __global__ void __launch_bounds__(256) project_bin_kernel(GeoT<T> G, const T *__
     }
     __syncthreads();
     T *col = library + (int64_t)p * G.rows;
-    for (int i = threadIdx.x; i < G.rows; i += blockDim.x) {
-        double v = (double)(long long)acc[i] * 0x1p-56;
-        if (i >= off_xy && i < off_h) v = v / (num_per_bin[i - off_xy] * area_pixel + kEps);
-        else if (i >= off_h) v = v / sg[(i - off_h) % nb];
-        col[i] = T(v);
+    if (sizeof(T) == 4) {
+        // float library: the entry and its normalisation in float (a product with the
+        // rounded reciprocal, within 1.5 float ulp of the quotient), so that the FP64
+        // pipe, 1/64 of the FP32 rate here, does no division per entry
+        for (int i = threadIdx.x; i < G.rows; i += blockDim.x) {
+            float v = (float)(long long)acc[i] * 0x1p-56f;
+            if (i >= off_xy && i < off_h) v *= 1.0f / (float)(num_per_bin[i - off_xy] * area_pixel + kEps);
+            else if (i >= off_h) v *= 1.0f / (float)sg[(i - off_h) % nb];
+            col[i] = T(v);
+        }
+    } else {
+        for (int i = threadIdx.x; i < G.rows; i += blockDim.x) {
+            double v = (double)(long long)acc[i] * 0x1p-56;
+            if (i >= off_xy && i < off_h) v = v / (num_per_bin[i - off_xy] * area_pixel + kEps);
+            else if (i >= off_h) v = v / sg[(i - off_h) % nb];
+            col[i] = T(v);
+        }
     }
 }
 

@@ -58,7 +58,7 @@ __global__ void __launch_bounds__(256) gj_diag_kernel(const float *__restrict__ 
     for (int e = threadIdx.x; e < GJ_B * GJ_B; e += blockDim.x) P[e] = s[e % GJ_B][e / GJ_B];
 }
 
-// R (64 x mp, column-major ld 64) = P A[k block rows, :]; grid over 128-column tiles
+// R (64 x mp, row r at R + mp r) = P A[k block rows, :]; grid over 128-column tiles
 __global__ void __launch_bounds__(256) gj_row_kernel(const float *__restrict__ A, int64_t ld, int64_t k0,
                                                      const float *__restrict__ P, float *R) {
     __shared__ float sp[GJ_B][GJ_B + 1];
@@ -70,34 +70,32 @@ __global__ void __launch_bounds__(256) gj_row_kernel(const float *__restrict__ A
         sa[r][c] = A[(k0 + r) + ld * (j0 + c)];
     }
     __syncthreads();
-    // each thread: row r = tid % 64, columns c = tid / 64 + 4 q
-    const int r = threadIdx.x % GJ_B;
-    for (int c = threadIdx.x / GJ_B; c < GJ_T; c += 4) {
+    // each thread: column c = tid % 128, rows r = tid / 128 + 2 q (consecutive threads
+    // write consecutive columns of a row)
+    const int c = threadIdx.x % GJ_T;
+    for (int r = threadIdx.x / GJ_T; r < GJ_B; r += 2) {
         float acc = 0.f;
 #pragma unroll 16
         for (int l = 0; l < GJ_B; ++l) acc += sp[r][l] * sa[l][c];
-        R[r + (int64_t)GJ_B * (j0 + c)] = acc;
+        R[(j0 + c) + ld * r] = acc;
     }
 }
 
 // A_ij -= A_ik R_kj for the 128 x 128 tile (blockIdx.x, blockIdx.y), skipping the
-// rows and columns of block k; 8 x 8 outputs per thread
+// rows and columns of block k.  Thread (tx, ty) of 16 x 16 owns rows 8 tx .. 8 tx + 7
+// (contiguous, read and written as float4) of columns ty + 16 b, b < 8; both panels are
+// staged in shared memory with coalesced loads (R row-major: R[j + ld l]).
 __global__ void __launch_bounds__(256) gj_update_kernel(float *A, int64_t ld, int64_t k0, const float *__restrict__ R) {
-    __shared__ float sc[GJ_B][GJ_T + 4];   // sc[l][i]: A[i0 + i, k0 + l]
-    __shared__ float sr[GJ_B][GJ_T + 4];   // sr[l][j]: R[l, j0 + j]
+    __shared__ __align__(16) float sc[GJ_B][GJ_T];   // sc[l][i]: A[i0 + i, k0 + l]
+    __shared__ __align__(16) float sr[GJ_B][GJ_T];   // sr[l][j]: R[l, j0 + j]
     const int64_t i0 = (int64_t)blockIdx.x * GJ_T, j0 = (int64_t)blockIdx.y * GJ_T;
-    const bool rows_hit = (k0 >= i0 && k0 < i0 + GJ_T), cols_hit = (k0 >= j0 && k0 < j0 + GJ_T);
-    if (rows_hit && cols_hit && GJ_T == 2 * GJ_B) {
-        // the tile holds the 64 x 64 diagonal block; its other three quarters are
-        // still updated below
-    }
-    for (int e = threadIdx.x; e < GJ_B * GJ_T; e += blockDim.x) {
-        const int i = e % GJ_T, l = e / GJ_T;
-        sc[l][i] = A[(i0 + i) + ld * (k0 + l)];
-        sr[l][i] = R[l + (int64_t)GJ_B * (j0 + i)];
+    for (int e = threadIdx.x; e < GJ_B * GJ_T / 4; e += blockDim.x) {
+        const int i4 = e % (GJ_T / 4), l = e / (GJ_T / 4);
+        *(float4 *)&sc[l][4 * i4] = *(const float4 *)&A[(i0 + 4 * i4) + ld * (k0 + l)];
+        *(float4 *)&sr[l][4 * i4] = *(const float4 *)&R[(j0 + 4 * i4) + ld * l];
     }
     __syncthreads();
-    const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;   // 16 x 16 threads, 8 x 8 each
+    const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
     float acc[8][8];
 #pragma unroll
     for (int a = 0; a < 8; ++a)
@@ -106,8 +104,9 @@ __global__ void __launch_bounds__(256) gj_update_kernel(float *A, int64_t ld, in
 #pragma unroll 4
     for (int l = 0; l < GJ_B; ++l) {
         float ci[8], rj[8];
-#pragma unroll
-        for (int a = 0; a < 8; ++a) ci[a] = sc[l][tx + 16 * a];
+        const float4 c0 = *(const float4 *)&sc[l][8 * tx], c1 = *(const float4 *)&sc[l][8 * tx + 4];
+        ci[0] = c0.x; ci[1] = c0.y; ci[2] = c0.z; ci[3] = c0.w;
+        ci[4] = c1.x; ci[5] = c1.y; ci[6] = c1.z; ci[7] = c1.w;
 #pragma unroll
         for (int b = 0; b < 8; ++b) rj[b] = sr[l][ty + 16 * b];
 #pragma unroll
@@ -115,16 +114,18 @@ __global__ void __launch_bounds__(256) gj_update_kernel(float *A, int64_t ld, in
 #pragma unroll
             for (int b = 0; b < 8; ++b) acc[a][b] += ci[a] * rj[b];
     }
+    const int64_t ib = i0 + 8 * tx;
+    const bool rows_in_k = ib >= k0 && ib < k0 + GJ_B;   // 8-row groups lie inside or outside block k
 #pragma unroll
     for (int b = 0; b < 8; ++b) {
         const int64_t j = j0 + ty + 16 * b;
-        if (j >= k0 && j < k0 + GJ_B) continue;
-#pragma unroll
-        for (int a = 0; a < 8; ++a) {
-            const int64_t i = i0 + tx + 16 * a;
-            if (i >= k0 && i < k0 + GJ_B) continue;
-            A[i + ld * j] -= acc[a][b];
-        }
+        if (rows_in_k || (j >= k0 && j < k0 + GJ_B)) continue;
+        float4 *p = (float4 *)&A[ib + ld * j];
+        float4 v0 = p[0], v1 = p[1];
+        v0.x -= acc[0][b]; v0.y -= acc[1][b]; v0.z -= acc[2][b]; v0.w -= acc[3][b];
+        v1.x -= acc[4][b]; v1.y -= acc[5][b]; v1.z -= acc[6][b]; v1.w -= acc[7][b];
+        p[0] = v0;
+        p[1] = v1;
     }
 }
 
@@ -161,7 +162,7 @@ __global__ void gj_copy_kernel(float *A, int64_t ld, int64_t k0, const float *__
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < GJ_B * mp; e += (int64_t)gridDim.x * blockDim.x) {
         const int64_t r = e % GJ_B, j = e / GJ_B;
         if (j >= k0 && j < k0 + GJ_B) continue;
-        A[(k0 + r) + ld * j] = R[e];
+        A[(k0 + r) + ld * j] = R[j + ld * r];
     }
 }
 

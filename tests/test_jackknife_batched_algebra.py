@@ -107,6 +107,66 @@ def _batched(p, n_groups, lam, maxiter, tol=1e-17, max_terms=200):
     return Z, max(r["delta"] / k for r in reps), max(terms)
 
 
+def _batched_h(p, n_groups, lam, maxiter, tol=1e-12):
+    """The form the kernels iterate: H = X U once, then per replicate and iteration
+    W = sum_t (delta S)^t E (S = G_KK^-1, E = y_g - U_g D, zero on d) and
+    w = D + U^T S W = D + H^T W - H_d^T X_dd^-1 (X W)_d, since W vanishes on d."""
+    U = onnls.design(p["A_rz"], p["A_xy"], *p["A_h"], p["gamma"], p["sig_rz"], p["sig_xy"], *p["sh"], **W)
+    y = onnls.rhs_vector(p["y_rz"], p["y_xy"], *p["yh"], p["sig_rz"], p["sig_xy"], *p["sh"], **W)
+    m, n = U.shape
+    nc, nb = p["nc"], p["nb"]
+    nrm2 = float(np.sum(U * U))
+    k = lam / n + (nrm2 + lam) / n
+    X = np.linalg.inv(k * np.eye(m) + U @ U.T)
+    H = X @ U
+    grp = np.arange(nb) % n_groups
+    w0 = np.sum(p["y_rz"]) / n
+    Z = np.full((n_groups, n), w0)
+    Uu = np.zeros((n_groups, n))
+    reps = []
+    for g in range(n_groups):
+        bins = np.nonzero(grp == g)[0]
+        d = np.concatenate([nc + j * nb + bins for j in range(5)])
+        keep = np.ones(m, bool)
+        keep[d] = False
+        rho = (nrm2 - float(np.sum(U[d] ** 2)) + lam) / n
+        kg = lam / n + rho
+        reps.append(dict(d=d, keep=keep, rho=rho, kg=kg, delta=k - kg, Xdd_inv=np.linalg.inv(X[np.ix_(d, d)])))
+    q = max(r["delta"] / k for r in reps)
+    terms = 1
+    while q ** terms > tol:
+        terms += 1
+
+    def s_apply(r, v):                      # S v = X v - X_{:,d} X_dd^-1 (X v)_d, zero on d
+        t = X @ v
+        return t - X[:, r["d"]] @ (r["Xdd_inv"] @ t[r["d"]])
+
+    for _ in range(maxiter):
+        for g, r in enumerate(reps):
+            D = (r["rho"] / r["kg"]) * (Z[g] - Uu[g])
+            e = (y - U @ D) * r["keep"]
+            v, Wg = e, e.copy()
+            for _t in range(1, terms):
+                v = r["delta"] * s_apply(r, v)
+                Wg += v
+            c = r["Xdd_inv"] @ (X[r["d"]] @ Wg)
+            w = D + H.T @ Wg - H[r["d"]].T @ c
+            wh = 1.6 * w - 0.6 * Z[g]
+            zn = np.maximum(0.0, wh + Uu[g])
+            Uu[g] = Uu[g] + wh - zn
+            Z[g] = zn
+    return Z, terms
+
+
+def test_h_form_of_the_batched_jackknife():
+    p = _problem(seed=2, nb=16)
+    lam, it = 1.0, 120
+    ref = _reference(p, p["nb"], lam, it)
+    got, terms = _batched_h(p, p["nb"], lam, it)
+    np.testing.assert_allclose(got, ref, rtol=0, atol=1e-9 * np.abs(ref).max())
+    assert terms >= 2
+
+
 def test_batched_jackknife_matches_per_replicate_solves():
     p = _problem()
     lam, it = 1.0, 200
