@@ -130,6 +130,7 @@ def run_ours(args, rank, world, local):
     dict_data, theta = synthetic.make_dataset(cfg, seed=args.seed)
     setup_s = time.time() - t0
     st = cfg.settings("mixed")
+    st.bootstrap = args.bootstrap
     dd = engine.DeviceData(dict_data, n_real=st.n_real)
     nb = cfg.n_bins
     nc = cfg.n_grid[0] * cfg.n_grid[1] * cfg.n_grid[2]
@@ -199,7 +200,7 @@ def run_ours(args, rank, world, local):
                 "flops_per_attempt": 3 * FLOPS_PER_FORCE + FLOPS_PER_STEP}
     # --- precision: mixed NNLS vs FP64 NNLS on the same library, and plain FP64 -------
     prec = {}
-    if rank == 0 and not args.skip_fp64:
+    if rank == 0 and not args.skip_fp64 and args.bootstrap == "gaussian":
         prec = precision_and_fp64(cfg, dd, grid, nb, theta, st, step, value / world)
     # --- end to end through the public API with host buffers ------------------------------
     e2e = None
@@ -228,7 +229,7 @@ def run_ours(args, rank, world, local):
                 "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32 (orbits, binning) / bf16 split products + f64 (NNLS)",
                 "data": "synthetic (seeded; schwarmax_gb300.synthetic)",
-                "config": {"workload": WORKLOAD, "parallelism": f"replicas x{world}",
+                "config": {"workload": WORKLOAD, "bootstrap": args.bootstrap, "parallelism": f"replicas x{world}",
                            "l2": "working set > L2 (no flush)", "setup_s": round(setup_s, 1)},
                 "gpu_launches": int(launches), "roofline": roofline, "stages_ms": stages, "precision": prec, "e2e": e2e,
                 "cpu_baseline": cpu, "clocks": clocks, "logL_last": float(val.item())}
@@ -266,6 +267,7 @@ def run_batch(args, rank, world, local):
     setup_s = time.time() - t0
     st = cfg.settings("mixed")
     st.autotune = not args.no_autotune
+    st.bootstrap = args.bootstrap
     dd = engine.DeviceData(dict_data, n_real=st.n_real)
     nb = cfg.n_bins
     nc = cfg.n_grid[0] * cfg.n_grid[1] * cfg.n_grid[2]
@@ -368,7 +370,7 @@ def run_batch(args, rank, world, local):
     if rank == 0:
         torch.cuda.empty_cache()
         # precision and the plain FP64 denominator on point 0 of the batch
-        if not args.skip_fp64:
+        if not args.skip_fp64 and args.bootstrap == "gaussian":
             th0 = points[0].copy()
 
             def single(i):
@@ -403,7 +405,8 @@ def run_batch(args, rank, world, local):
                 "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32 (orbits, binning) / bf16 split products + f64 (NNLS)",
                 "data": "synthetic (seeded; schwarmax_gb300.synthetic)",
-                "config": {"workload": WORKLOAD_BATCH.format(P=P, jk=""), "evals_per_step": P,
+                "config": {"workload": WORKLOAD_BATCH.format(P=P, jk=""), "bootstrap": args.bootstrap,
+                           "evals_per_step": P,
                            "parallelism": f"replicas x{world}", "l2": "working set > L2 (no flush)",
                            "setup_s": round(setup_s, 1), "autotune": st.autotune},
                 "gpu_launches": int(launches), "roofline": roofline, "e2e": e2e, "cpu_baseline": cpu,
@@ -826,6 +829,7 @@ def adjoint_timing(dict_data, theta, cfg, st):
     prob, th0 = adjoint.problem_from_evaluation(theta, dict_data, cfg.n_bins,
                                                 cfg.n_grid[0] * cfg.n_grid[1] * cfg.n_grid[2], settings=st,
                                                 sigma_pix=0.5, precision="mixed")
+    prob.admm_iters = 3000      # a converged ADMM start: the active-set steps then have little to do
     th = th0 + np.array([0.05, -0.05, 0.05, 0.05])
     prob.chi2_and_grad(th)
     torch.cuda.synchronize()
@@ -835,10 +839,10 @@ def adjoint_timing(dict_data, theta, cfg, st):
     torch.cuda.synchronize()
     t_grad = time.time() - t0
 
-    def free_set(t):
+    def chi2_and_free_set(t):
         lib = prob.soft_library(t)
-        _, idx, _ = prob.solve(lib, prob.design(lib))
-        return set(idx.cpu().numpy().tolist())
+        w, idx, _ = prob.solve(lib, prob.design(lib))
+        return float(prob.chi2_of_model(lib.t() @ w)), set(idx.cpu().numpy().tolist())
 
     checks = []
     d10 = np.radians(10.0)
@@ -848,16 +852,18 @@ def adjoint_timing(dict_data, theta, cfg, st):
         t[3] = th0[3] * vs
         c, gr = prob.chi2_and_grad(t)
         gr = gr.cpu().numpy()
+        settled = bool(prob.kkt_settled)
         rows = []
         for k in range(4):
             h = 1e-5 if k < 3 else 1e-5 * t[3]
             e = np.zeros(4)
             e[k] = h
-            fd = (prob.chi2(t + e) - prob.chi2(t - e)) / (2 * h)
+            (cp, fp), (cm, fm) = chi2_and_free_set(t + e), chi2_and_free_set(t - e)
+            fd = (cp - cm) / (2 * h)
             rows.append({"grad": float(gr[k]), "fd": float(fd),
-                         "rel_err": float(abs(gr[k] - fd) / max(abs(fd), 1e-300)),
-                         "free_set_changes": free_set(t + e) != free_set(t - e)})
+                         "rel_err": float(abs(gr[k] - fd) / max(abs(fd), 1e-300)), "free_set_changes": fp != fm})
         checks.append({"angles_shift_deg": float(np.degrees(shift)), "vscale": float(t[3]), "chi2": c,
+                       "kkt_settled": settled,
                        "alpha": rows[0], "beta": rows[1], "gamma": rows[2], "vscale_grad": rows[3]})
     return {"workload": "config3: soft apertures (sigma 0.5 px) on the stored orbits of one config-1 evaluation, "
                         "single data row, FP64 soft projection, ADMM + active-set KKT NNLS; the gradient is that of "
@@ -890,6 +896,9 @@ def main():
     ap.add_argument("--critical-path", action="store_true",
                     help="--config 1: time the integrator launch in queue order and in cost order, and the longest "
                          "orbits alone (32, 4,864 and 19,456 of them), and print them with the attempt statistics")
+    ap.add_argument("--bootstrap", default="gaussian", choices=["gaussian", "poisson"],
+                    help="gaussian: the reference's perturbed data rows (one shared solve for all resamples); "
+                         "poisson: Poisson(1) aperture weights per resample (one solve each)")
     ap.add_argument("--jackknife-points", type=int, default=1,
                     help="--config 2: points of the batch whose 400-replicate leave-one-bin-out jackknife is timed")
     ap.add_argument("--adjoint", action="store_true",

@@ -63,6 +63,16 @@ typedef struct {
     double bar_M, bar_a, bar_b, bar_L, bar_gamma;             /* T3 by default */
     double bulge_M, bulge_a, bulge_b, bulge_L, bulge_gamma;   /* V4 by default */
     int bar_type, bulge_type;                                 /* SMX_DEHNEN_* (0: default) */
+    /* Optional cylindrical-spline component (CylindricalSpline.py:354-519), added to the
+     * potential and the forces (not to the stellar density); cyl_n_modes = 0 leaves it
+     * out.  The table is get_phi_m's (CylindricalSpline.py:270-352) in DEVICE memory:
+     * cyl_r_grid (cyl_n_r), cyl_z_grid (cyl_n_z): increasing, in asinh(R/cyl_r0) and
+     * asinh(|z|/cyl_r0); cyl_coef (cyl_n_modes, 6, cyl_n_r, cyl_n_z): for m = 0 .. n-1,
+     * Phi_m_real, Phi_m_img, Mx_real, My_real, Mx_img, My_img.  Outside the grid the
+     * component is 0, as in the reference's fill value. */
+    int cyl_n_r, cyl_n_z, cyl_n_modes;
+    double cyl_r0;
+    const double *cyl_r_grid, *cyl_z_grid, *cyl_coef;
 } smx_potential;
 
 /* One parameter point of a batched call: its potential and the frame's angular

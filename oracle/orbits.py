@@ -66,4 +66,5 @@ def jitter(w0_new, Vc, uniforms):
 def jacobi_energy(w, P, Omega):
     x, y, z, vx, vy, vz = (w[..., i] for i in range(6))
     ek = 0.5 * (vx ** 2 + vy ** 2 + vz ** 2)
-    return ek + pot.phi(x, y, z, P) - Omega * (x * vy - y * vx)
+    phi = pot.phi_acc(x, y, z, P)[0] if P.get("cylspline") is not None else pot.phi(x, y, z, P)
+    return ek + phi - Omega * (x * vy - y * vx)

@@ -338,12 +338,18 @@ def rho(x, y, z, P):
 
 def acc(x, y, z, P):
     """-grad Phi (model.py:152-157), exact forward-mode derivative."""
-    X, Y, Zc = D.seed(x, y, z)
-    p = phi(X, Y, Zc, P)
-    return -p.d[0], -p.d[1], -p.d[2]
+    _, ax, ay, az = phi_acc(x, y, z, P)
+    return ax, ay, az
 
 
 def phi_acc(x, y, z, P):
+    """Phi and -grad Phi; P["cylspline"] (get_phi_m's table, optional) adds the
+    cylindrical-spline component (oracle/cylspline.py)."""
     X, Y, Zc = D.seed(x, y, z)
     p = phi(X, Y, Zc, P)
-    return p.v, -p.d[0], -p.d[1], -p.d[2]
+    out = (p.v, -p.d[0], -p.d[1], -p.d[2])
+    if P.get("cylspline") is not None:
+        from . import cylspline
+        cp, ca = cylspline.phi_and_acc(x, y, z, P["cylspline"])
+        out = (out[0] + cp, out[1] + ca[0], out[2] + ca[1], out[3] + ca[2])
+    return out

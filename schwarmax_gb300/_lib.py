@@ -92,8 +92,10 @@ class SmxPotential(ctypes.Structure):
     _fields_ = [(n, ctypes.c_double) for n in (
         "halo_M", "halo_Rs", "halo_qa", "halo_qb", "halo_qc", "disc_M", "disc_a", "disc_b",
         "bar_M", "bar_a", "bar_b", "bar_L", "bar_gamma",
-        "bulge_M", "bulge_a", "bulge_b", "bulge_L", "bulge_gamma")] + [("bar_type", ctypes.c_int),
-                                                                      ("bulge_type", ctypes.c_int)]
+        "bulge_M", "bulge_a", "bulge_b", "bulge_L", "bulge_gamma")] + [
+        ("bar_type", ctypes.c_int), ("bulge_type", ctypes.c_int),
+        ("cyl_n_r", ctypes.c_int), ("cyl_n_z", ctypes.c_int), ("cyl_n_modes", ctypes.c_int), ("cyl_r0", ctypes.c_double),
+        ("cyl_r_grid", ctypes.c_void_p), ("cyl_z_grid", ctypes.c_void_p), ("cyl_coef", ctypes.c_void_p)]
 
 
 DEHNEN_TYPES = {"T1": 1, "T2": 2, "T3": 3, "T4": 4, "V1": 11, "V2": 12, "V3": 13, "V4": 14}

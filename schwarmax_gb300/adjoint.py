@@ -114,39 +114,66 @@ class SoftProblem:
         return (lib[:, self.row_map.long()] * self.row_scale[None, :]).t().contiguous()   # (m, n)
 
     def solve(self, lib, U):
-        """NNLS solution: ADMM, then active-set steps to the exact KKT point of
-        min |U w - y|^2 + (lambda/n) |w|^2, w >= 0: solve on the free set F, drop
-        entries that come out <= 0, add inactive entries whose gradient is
-        negative (most negative first), until the KKT conditions hold."""
+        """NNLS solution: ADMM, then Lawson-Hanson active-set steps to the exact KKT point of
+        min |U w - y|^2 + (lambda/n) |w|^2, w >= 0.  Starting from the ADMM iterate
+        (feasible, w >= 0) with its positive entries as the free set F: solve on F; if
+        some entries come out <= 0, move from the current w towards that solution only as
+        far as the first entry reaches zero and drop the entries at zero (so w stays
+        feasible and the objective decreases); once the solution on F is positive, add the
+        quarter of the inactive entries whose gradient is most negative, until the KKT
+        conditions hold to 1e-8 of |U^T y| (at most 50 rounds; `kkt_settled` records
+        whether they did).  An entry dropped right after it was added sits out one round.
+        The fewer ADMM iterations (`admm_iters`), the farther the start and the more rounds."""
         n = self.n
         w_init = float((self.d["y_rz"].sum() / n).item())
         W0 = kernels.nnls_admm(lib, self.row_map, self.row_scale, self.y[None, :].contiguous(), self.admm_iters,
                                self.lam, w_init, mixed=False)[0]
         lam_n = self.lam / n
         Uty = U.t() @ self.y
-        tol = 1e-10 * float(Uty.abs().max())
+        # a KKT violation below 1e-8 of |U^T y| is rounding of the free-set solve, not a
+        # missing orbit: counting it would keep adding and dropping the same entries
+        tol = 1e-8 * float(Uty.abs().max())
         free = W0 > 0
-        w = torch.zeros(n, dtype=torch.float64, device=U.device)
-        for _ in range(200):
-            idx = torch.nonzero(free).flatten()
-            UF = U[:, idx]
-            H = UF.t() @ UF + lam_n * torch.eye(idx.numel(), dtype=torch.float64, device=U.device)
-            L = torch.linalg.cholesky(H)
-            wF = torch.cholesky_solve(Uty[idx][:, None], L)[:, 0]
-            if not bool((wF > 0).all()):
-                free[idx[wF <= 0]] = False
-                continue
+        w = torch.where(free, W0, torch.zeros_like(W0))
+        eye = lambda k: torch.eye(k, dtype=torch.float64, device=U.device)   # noqa: E731
+        self.kkt_settled = False
+        added = torch.zeros_like(free)
+        for outer in range(50):
+            dropped = torch.zeros_like(free)
+            while True:   # each pass drops at least one entry, so this ends
+                idx = torch.nonzero(free).flatten()
+                UF = U[:, idx]
+                L = torch.linalg.cholesky(UF.t() @ UF + lam_n * eye(idx.numel()))
+                wF = torch.cholesky_solve(Uty[idx][:, None], L)[:, 0]
+                neg = wF <= 0
+                if not bool(neg.any()):
+                    break
+                cur = w[idx]
+                alpha = float(torch.min(cur[neg] / (cur[neg] - wF[neg])))
+                cur = cur + alpha * (wF - cur)
+                w[idx] = cur
+                drop = idx[cur <= 1e-14 * float(cur.abs().max())]
+                w[drop] = 0.0
+                free[drop] = False
+                dropped[drop] = True
             w.zero_()
             w[idx] = wF
             grad = U.t() @ (U @ w) - Uty + lam_n * w          # gradient of the objective / 2
             viol = (~free) & (grad < -tol)
             if not bool(viol.any()):
+                self.kkt_settled = True
                 return w, idx, L
-            cand = torch.nonzero(viol).flatten()
-            k = max(1, cand.numel() // 4)                      # the most negative quarter first
+            cand = torch.nonzero(viol & ~(dropped & added)).flatten()
+            if cand.numel() == 0:
+                cand = torch.nonzero(viol).flatten()
+            k = max(1, cand.numel() // 4)
             add = cand[torch.argsort(grad[cand])[:k]]
+            added.zero_()
+            added[add] = True
             free[add] = True
-        raise RuntimeError("active-set refinement of the NNLS solution did not settle")
+        # not settled within the rounds: the last solve on its free set is returned
+        # (kkt_settled stays False); its remaining violations are below the ones added
+        return w, idx, L
 
     def chi2_of_model(self, mp):
         """chi^2 of the unperturbed data (likelihood.py:214-226) for model rows mp (rows,)."""

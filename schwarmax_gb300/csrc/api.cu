@@ -49,6 +49,14 @@ int validate_potential(const smx_potential *p) {
     for (int t : {p->bar_type, p->bulge_type})
         if (!(t == 0 || (t >= 1 && t <= 4) || (t >= 11 && t <= 14)))
             return set_error(SMX_ERR_UNSUPPORTED, "Dehnen model type %d is not built (T1-T4, V1-V4)", t);
+    if (p->cyl_n_modes != 0) {
+        if (p->cyl_n_modes < 0 || p->cyl_n_modes > 64 || p->cyl_n_r < 4 || p->cyl_n_z < 4)
+            return set_error(SMX_ERR_ARGUMENT, "cylindrical spline: 1..64 modes and at least 4 grid points per axis");
+        if (!(p->cyl_r0 > 0) || !std::isfinite(p->cyl_r0))
+            return set_error(SMX_ERR_ARGUMENT, "cylindrical spline: r0 must be finite and > 0");
+        if (!p->cyl_r_grid || !p->cyl_z_grid || !p->cyl_coef)
+            return set_error(SMX_ERR_ARGUMENT, "cylindrical spline: NULL table");
+    }
     return SMX_OK;
 }
 

@@ -540,15 +540,21 @@ __global__ void ns_residual_kernel(unsigned long long *T, float *Racc, const int
     if ((threadIdx.x & 31) == 0) atomicAdd(rss, acc);
 }
 
-// X <- X + X R
-__global__ void ns_update_kernel(unsigned long long *T, float *Racc, const int32_t *eX, const int32_t *eR, double *X,
-                                 int64_t m, const int *skip, int t_shift) {
+// X <- X + X R.  X R = X - X G X is symmetric, so the product is formed on the lower
+// tiles only (tiles of split::MT rows) and an element of an upper tile takes the value
+// of its mirror; X stays exactly symmetric.  T and R are cleared by a separate pass
+// (a thread may read the mirror of an element another thread is done with).
+__global__ void ns_update_kernel(const unsigned long long *T, const float *Racc, const int32_t *eX,
+                                 const int32_t *eR, double *X, int64_t m, const int *skip, int t_shift) {
     if (*skip) return;
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < m * m; k += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t r = k % m, col = k / m;
-        X[k] += product_value(T, Racc, k, eX[r], eR[col], t_shift);
-        T[k] = 0ull;
-        Racc[k] = 0.0f;
+        int64_t i = k % m, j = k / m;
+        if (j / split::MT > i / split::MT) {
+            const int64_t t = i;
+            i = j;
+            j = t;
+        }
+        X[k] += product_value(T, Racc, i + m * j, eX[i], eR[j], t_shift);
     }
 }
 
@@ -685,12 +691,10 @@ static int mixed_setup(const smx_nnls_problem *p, const TL *lib, const int32_t *
     count_launch();
     const int *skip = nsf + 3;
     for (int step = 0; step < kNsMaxSteps; ++step) {
-        // The first step starts from the float seed (||I - G X0|| ~ 2e-3): its output is
-        // only as good as ||R0||^2 ~ 4e-6, so its products keep 3 slices (23 bits, errors
-        // ~1e-7 after the cond(G) ~ 2e3 amplification of the update); later steps use 7
-        // (residual) and 5 (update).  A poorer seed costs one more full step, not accuracy.
-        split::Operand g = sh.G7, x = sh.X7, xr = sh.X5, rr = sh.R5;
-        if (step == 0) g.S = x.S = xr.S = rr.S = 3;
+        // Residual products keep 7 slices and updates 5 in every step: a first step with
+        // 3-slice products (its output only needs to be as good as ||R0||^2 ~ 4e-6) left a
+        // residual too large for the second step to be the last, and so cost a third step.
+        const split::Operand &g = sh.G7, &x = sh.X7, &xr = sh.X5, &rr = sh.R5;
         if ((st = split::slice_rows<double>(Xd, m, 1, sh.X7, rowmax, s, true, skip))) return st;   // O_X columns over k
         if ((st = split::gemm(g, x, acc, false, derr, s, 0, skip))) return st;
         SMX_TRY_CUDA(cudaMemsetAsync(rss, 0, sizeof(double), s));
@@ -700,11 +704,12 @@ static int mixed_setup(const smx_nnls_problem *p, const TL *lib, const int32_t *
         count_launch(2);
         if ((st = split::slice_rows<double>(Xd, 1, m, sh.X5, rowmax, s, false, skip))) return st;   // X rows over k
         if ((st = split::slice_rows<double>(Rd, m, 1, sh.R5, rowmax, s, false, skip))) return st;   // R columns over k
-        if ((st = split::gemm(xr, rr, acc, false, derr, s, 0, skip))) return st;
+        if ((st = split::gemm(xr, rr, acc, true, derr, s, 0, skip))) return st;
         ns_update_kernel<<<grid1d(m * m), 256, 0, s>>>(Tacc, Racc, sh.X5.expo, sh.R5.expo, Xd, m, skip,
                                                        8 * (split::exact_levels(xr, rr) - 1));
+        clear_kernel<<<grid1d(m * m), 256, 0, s>>>(Tacc, Racc, m * m);
         ns_skip_kernel<<<1, 1, 0, s>>>(nsf);
-        count_launch(2);
+        count_launch(3);
     }
     ns_verdict_kernel<<<1, 1, 0, s>>>(nsf, dinfo);
     count_launch();
@@ -716,8 +721,10 @@ static int mixed_setup(const smx_nnls_problem *p, const TL *lib, const int32_t *
         // H = G^-1 U, once per solve: every iteration then needs U D and H^T E only
         // (w = D + H^T (y - U D)), in place of U D, G^-1 E and U^T F.  U is overwritten
         // by H, and the slices of U^T (orbits over rows) by those of H^T.
+        // pairs s + t <= 6: the pairs left out weigh 2^-40 of max|O| max|U| per term, far
+        // below the 31-bit slicing of U and of H itself
         split::Acc acc_h{Tacc, Racc, m};
-        if ((st = split::gemm(sh.Xg, sh.Ut, acc_h, false, derr, s))) return st;   // O U
+        if ((st = split::gemm(sh.Xg, sh.Ut, acc_h, false, derr, s, 6))) return st;   // O U
         h_combine_kernel<<<grid1d(m * n), 256, 0, s>>>(Tacc, Racc, sh.Xg.expo, sh.Ut.expo, gdiag, U, m, n);
         count_launch();
         if ((st = split::slice_rows<double>(U, m, 1, sh.Ut, rowmax, s))) return st;   // H^T: orbits over rows

@@ -35,7 +35,9 @@ __global__ void potential_eval_kernel(PotT<T> P, const T *__restrict__ x, const 
 // One warp per particle.  jeans.py:8-93 with the vertical integrals split over
 // the 32 lanes (1000 trapezoid points each), then utils.py:182-273 for V_c and
 // T_orb at the new (R, z) and the jitter of model.py:127-148.
-template <typename T>
+// CANON: the bar and bulge slots hold T3 / V4 and there is no spline component (the
+// compile-time path of the potential, as in the integrator).
+template <typename T, bool CANON>
 __global__ void initial_conditions_kernel(PotT<T> P, const T *__restrict__ pos, const T *__restrict__ normals,
                                           const T *__restrict__ unif, int64_t n, int n_real, T n_periods,
                                           T steps_pp, T *w_out, T *t_total, T *dt_init, T *w0_new, T *t_orb,
@@ -57,10 +59,10 @@ __global__ void initial_conditions_kernel(PotT<T> P, const T *__restrict__ pos, 
     for (int j = lane; j < NQ; j += 32) {
         const T zj = (j == NQ - 1) ? ztop : za + T(j) * dzq;
         const T wj = (j == 0 || j == NQ - 1) ? T(0.5) : T(1);
-        const T f0 = density(P, x, y, zj) * (phi_only(P, x, y, zj + d) - phi_only(P, x, y, zj - d)) * i2d;
+        const T f0 = density(P, x, y, zj) * (phi_only<T, CANON>(P, x, y, zj + d) - phi_only<T, CANON>(P, x, y, zj - d)) * i2d;
         const T Rp = R + d, Rm = R - d;
-        const T fp = density(P, Rp, zero, zj) * (phi_only(P, Rp, zero, zj + d) - phi_only(P, Rp, zero, zj - d)) * i2d;
-        const T fm = density(P, Rm, zero, zj) * (phi_only(P, Rm, zero, zj + d) - phi_only(P, Rm, zero, zj - d)) * i2d;
+        const T fp = density(P, Rp, zero, zj) * (phi_only<T, CANON>(P, Rp, zero, zj + d) - phi_only<T, CANON>(P, Rp, zero, zj - d)) * i2d;
+        const T fm = density(P, Rm, zero, zj) * (phi_only<T, CANON>(P, Rm, zero, zj + d) - phi_only<T, CANON>(P, Rm, zero, zj - d)) * i2d;
         s0 += wj * f0;
         sp += wj * fp;
         sm += wj * fm;
@@ -76,7 +78,7 @@ __global__ void initial_conditions_kernel(PotT<T> P, const T *__restrict__ pos, 
         sz = M<T>::sqrt(sz2);
         sR = sz;   // anisotropy b = 1
         const T dP = (sp - sm) * i2d;
-        const T dphidR = (phi_only(P, R + d, zero, z) - phi_only(P, R - d, zero, z)) * i2d;
+        const T dphidR = (phi_only<T, CANON>(P, R + d, zero, z) - phi_only<T, CANON>(P, R - d, zero, z)) * i2d;
         const T vphi2 = sz2 + (R / nu) * dP + R * dphidR;
         const T vs2 = vphi2 - sR * sR;
         vstream = vs2 > T(0) ? M<T>::sqrt(vs2) : T(0);
@@ -95,7 +97,7 @@ __global__ void initial_conditions_kernel(PotT<T> P, const T *__restrict__ pos, 
     const T Rn = M<T>::sqrt(w[0] * w[0] + w[1] * w[1]);
     const T hR = T(1e-3);
     const T Rs = Rn > T(2) * hR ? Rn : T(2) * hR;
-    const T dphi = (phi_only(P, Rs + hR, zero, z) - phi_only(P, Rs - hR, zero, z)) / (T(2) * hR);
+    const T dphi = (phi_only<T, CANON>(P, Rs + hR, zero, z) - phi_only<T, CANON>(P, Rs - hR, zero, z)) / (T(2) * hR);
     const T vc2 = Rs * dphi;
     const T Vc = vc2 > T(0) ? M<T>::sqrt(vc2) : T(0);
     T om2 = M<T>::abs(dphi) / Rs;
@@ -186,15 +188,20 @@ int smx_initial_conditions(const smx_potential *pot, int precision, const void *
     cudaStream_t s = (cudaStream_t)stream;
     const int bs = 128;
     const unsigned grid = blocks_for(n * 32, bs);
+    const bool canon = canonical_types(*pot);
     if (precision == SMX_FP32) {
-        initial_conditions_kernel<float><<<grid, bs, 0, s>>>(make_pot<float>(*pot), (const float *)pos,
-            (const float *)normals, (const float *)uniforms, n, n_real, (float)n_periods, (float)steps_per_period,
-            (float *)w_out, (float *)t_total, (float *)dt_init, (float *)w0_new, (float *)t_orb, (float *)vc);
+        auto kern = canon ? initial_conditions_kernel<float, true> : initial_conditions_kernel<float, false>;
+        kern<<<grid, bs, 0, s>>>(make_pot<float>(*pot), (const float *)pos, (const float *)normals,
+                                 (const float *)uniforms, n, n_real, (float)n_periods, (float)steps_per_period,
+                                 (float *)w_out, (float *)t_total, (float *)dt_init, (float *)w0_new, (float *)t_orb,
+                                 (float *)vc);
         count_launch();
     } else if (precision == SMX_FP64) {
-        initial_conditions_kernel<double><<<grid, bs, 0, s>>>(make_pot<double>(*pot), (const double *)pos,
-            (const double *)normals, (const double *)uniforms, n, n_real, n_periods, steps_per_period,
-            (double *)w_out, (double *)t_total, (double *)dt_init, (double *)w0_new, (double *)t_orb, (double *)vc);
+        auto kern = canon ? initial_conditions_kernel<double, true> : initial_conditions_kernel<double, false>;
+        kern<<<grid, bs, 0, s>>>(make_pot<double>(*pot), (const double *)pos, (const double *)normals,
+                                 (const double *)uniforms, n, n_real, n_periods, steps_per_period, (double *)w_out,
+                                 (double *)t_total, (double *)dt_init, (double *)w0_new, (double *)t_orb,
+                                 (double *)vc);
         count_launch();
     } else {
         return set_error(SMX_ERR_ARGUMENT, "bad precision %d", precision);

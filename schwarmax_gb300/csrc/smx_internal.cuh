@@ -45,6 +45,7 @@ template <> struct M<float> {
     static __device__ __forceinline__ float rcbrt(float x) { return rcbrtf(x); }
     static __device__ __forceinline__ float exp(float x) { return expf(x); }
     static __device__ __forceinline__ float atan2(float y, float x) { return atan2f(y, x); }
+    static __device__ __forceinline__ float asinh(float x) { return asinhf(x); }
     static __device__ __forceinline__ float abs(float x) { return fabsf(x); }
     // fast reciprocal (max 2 ulp) and square root of a positive argument (x rsqrt(x),
     // about 3 ulp): the exact forms cost several instructions each, and the force
@@ -60,6 +61,7 @@ template <> struct M<double> {
     static __device__ __forceinline__ double rcbrt(double x) { return ::rcbrt(x); }
     static __device__ __forceinline__ double exp(double x) { return ::exp(x); }
     static __device__ __forceinline__ double atan2(double y, double x) { return ::atan2(y, x); }
+    static __device__ __forceinline__ double asinh(double x) { return ::asinh(x); }
     static __device__ __forceinline__ double abs(double x) { return ::fabs(x); }
     static __device__ __forceinline__ double rcp(double x) { return 1.0 / x; }
     static __device__ __forceinline__ double sqrt_pos(double x) { return ::sqrt(x); }
@@ -89,6 +91,9 @@ template <typename T> struct PotT {
     T ua, ub2, uL, uc1, uc2;                       // V4 bulge
     T ua3;                                         // bulge a/3 (for a T3 in the bulge slot)
     int btype, utype;                              // Dehnen model of each slot (0: T3 / V4)
+    int cyl_nr, cyl_nz, cyl_nm;                    // cylindrical-spline table (cyl_nm = 0: none)
+    T cyl_r0;
+    const double *cyl_r, *cyl_z, *cyl_c;
 };
 
 template <typename T> __host__ __device__ inline PotT<T> make_pot(const smx_potential &p) {
@@ -116,6 +121,13 @@ template <typename T> __host__ __device__ inline PotT<T> make_pot(const smx_pote
     q.ua3 = T(p.bulge_a / 3.0);
     q.btype = p.bar_type == 0 ? 3 : p.bar_type;
     q.utype = p.bulge_type == 0 ? 14 : p.bulge_type;
+    q.cyl_nm = p.cyl_n_modes > 0 ? p.cyl_n_modes : 0;
+    q.cyl_nr = p.cyl_n_r;
+    q.cyl_nz = p.cyl_n_z;
+    q.cyl_r0 = T(p.cyl_n_modes > 0 ? p.cyl_r0 : 1.0);
+    q.cyl_r = p.cyl_r_grid;
+    q.cyl_z = p.cyl_z_grid;
+    q.cyl_c = p.cyl_coef;
     return q;
 }
 
@@ -388,6 +400,94 @@ __device__ __forceinline__ T dehnen_rho(int type, T a, T b2, T L, T c1, T c2, T 
     return (b2 * iz * iz * iz) * pref * S0;
 }
 
+// ------------------------------------------------------- cylindrical spline
+// Interval of a sorted grid holding v: searchsorted(g, v) - 1 clipped to [0, n - 2]
+// (CubicSpline.py:138-142), i.e. the first index with g >= v, minus one.
+template <typename T>
+__device__ __forceinline__ int grid_interval(const double *__restrict__ g, int n, T v) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (T(g[mid]) < v) lo = mid + 1;
+        else hi = mid;
+    }
+    lo -= 1;
+    return lo < 0 ? 0 : (lo > n - 2 ? n - 2 : lo);
+}
+
+// Phi and grad Phi of the cylindrical-spline expansion (CylindricalSpline.py:418-519):
+// Phi = sum_m f_m (Re Phi_m(Rs, zs) cos m phi - Im Phi_m sin m phi), f_0 = 1, f_m = 2,
+// with the separable bicubic of CubicSpline.py:202-305 on Rs = asinh(R/R0),
+// zs = asinh(|z|/R0); nothing is added outside the grid (the reference's fill value 0).
+// cos m phi and sin m phi come from x/R, y/R by the angle-addition recurrence.
+template <typename T, bool WANT_PHI, bool WANT_GRAD>
+__device__ __forceinline__ void cylspline(const PotT<T> &P, T x, T y, T z, T &phi, T &gx, T &gy, T &gz) {
+    const int nr = P.cyl_nr, nz = P.cyl_nz;
+    const T R = M<T>::sqrt(x * x + y * y), za = M<T>::abs(z), R0 = P.cyl_r0;
+    const T Rs = M<T>::asinh(R / R0), zs = M<T>::asinh(za / R0);
+    if (Rs < T(P.cyl_r[0]) || Rs > T(P.cyl_r[nr - 1]) || zs < T(P.cyl_z[0]) || zs > T(P.cyl_z[nz - 1])) return;
+    const int ix = grid_interval<T>(P.cyl_r, nr, Rs), iy = grid_interval<T>(P.cyl_z, nz, zs);
+    const T gx0 = T(P.cyl_r[ix]), hx = T(P.cyl_r[ix + 1]) - gx0;
+    const T gy0 = T(P.cyl_z[iy]), hy = T(P.cyl_z[iy + 1]) - gy0;
+    const T tx = (Rs - gx0) / hx, ty = (zs - gy0) / hy;
+    const T ux = T(1) - tx, uy = T(1) - ty;
+    const T cx = hx * hx / T(6), cy = hy * hy / T(6);
+    const T wx0 = ux * ux * ux - ux, wx1 = tx * tx * tx - tx;      // value weights of M_x
+    const T dx0 = T(-3) * ux * ux + T(1), dx1 = T(3) * tx * tx - T(1);
+    const T wy0 = uy * uy * uy - uy, wy1 = ty * ty * ty - ty;
+    const T dy0 = T(-3) * uy * uy + T(1), dy1 = T(3) * ty * ty - T(1);
+    const bool rpos = R > T(1e-12);
+    const T c1 = rpos ? x / R : T(1), s1 = rpos ? y / R : T(0);   // cos, sin of atan2(y, x)
+    const int64_t plane = (int64_t)nr * nz;
+    const int64_t k00 = (int64_t)ix * nz + iy;
+    T S = T(0), dS_R = T(0), dS_z = T(0), dS_p = T(0);
+    T cm = T(1), sm = T(0);
+    for (int m = 0; m < P.cyl_nm; ++m) {
+        const double *base = P.cyl_c + (int64_t)m * 6 * plane;
+        T val[2], dvx[2], dvy[2];
+#pragma unroll
+        for (int part = 0; part < 2; ++part) {   // 0: real, 1: imaginary
+            const double *v = base + part * plane, *Mx = base + (2 + 2 * part) * plane,
+                         *My = base + (3 + 2 * part) * plane;
+            const T z00 = T(v[k00]), z10 = T(v[k00 + nz]), z01 = T(v[k00 + 1]), z11 = T(v[k00 + nz + 1]);
+            const T a00 = T(Mx[k00]), a10 = T(Mx[k00 + nz]), a01 = T(Mx[k00 + 1]), a11 = T(Mx[k00 + nz + 1]);
+            const T b00 = T(My[k00]), b10 = T(My[k00 + nz]), b01 = T(My[k00 + 1]), b11 = T(My[k00 + nz + 1]);
+            const T f0 = ux * z00 + tx * z10 + (wx0 * a00 + wx1 * a10) * cx;
+            const T f1 = ux * z01 + tx * z11 + (wx0 * a01 + wx1 * a11) * cx;
+            const T m0 = ux * b00 + tx * b10, m1 = ux * b01 + tx * b11;
+            val[part] = uy * f0 + ty * f1 + (wy0 * m0 + wy1 * m1) * cy;
+            if (WANT_GRAD) {
+                const T df0 = (z10 - z00) + (dx0 * a00 + dx1 * a10) * cx;
+                const T df1 = (z11 - z01) + (dx0 * a01 + dx1 * a11) * cx;
+                dvx[part] = (uy * df0 + ty * df1 + (wy0 * (b10 - b00) + wy1 * (b11 - b01)) * cy) / hx;
+                dvy[part] = ((f1 - f0) + (dy0 * m0 + dy1 * m1) * cy) / hy;
+            }
+        }
+        const T f = m == 0 ? T(1) : T(2);
+        S += f * (val[0] * cm - val[1] * sm);
+        if (WANT_GRAD) {
+            dS_R += f * (dvx[0] * cm - dvx[1] * sm);
+            dS_z += f * (dvy[0] * cm - dvy[1] * sm);
+            dS_p += f * (-T(m) * val[0] * sm - T(m) * val[1] * cm);
+        }
+        const T cn = cm * c1 - sm * s1;
+        sm = sm * c1 + cm * s1;
+        cm = cn;
+    }
+    if (WANT_PHI) phi += S;
+    if (WANT_GRAD) {
+        const T dphi_dR = dS_R / M<T>::sqrt(R * R + R0 * R0);
+        const T sz = z > T(0) ? T(1) : (z < T(0) ? T(-1) : T(0));
+        const T dphi_dz = dS_z / M<T>::sqrt(za * za + R0 * R0) * sz;
+        if (rpos) {
+            const T invR = T(1) / R;
+            gx += dphi_dR * (x * invR) + dS_p * (-y * invR * invR);
+            gy += dphi_dR * (y * invR) + dS_p * (x * invR * invR);
+        }
+        gz += dphi_dz;
+    }
+}
+
 // ------------------------------------------------------------- potential
 // Phi and/or its gradient (dPhi/dx, ...) of the canonical model at (x, y, z).
 // CANON: the bar and bulge slots hold their default models (T3, V4), fixed at
@@ -430,6 +530,7 @@ __device__ __forceinline__ void potential(const PotT<T> &P, T x, T y, T z, T &ph
                                                       gx, gy, gz);
     dehnen_phi<T, WANT_PHI, WANT_GRAD, CANON ? 14 : 0>(P.utype, P.ua, P.ua3, P.ub2, P.uL, P.uc1, P.uc2, x, y, z, phi,
                                                        gx, gy, gz);
+    if (!CANON && P.cyl_nm > 0) cylspline<T, WANT_PHI, WANT_GRAD>(P, x, y, z, phi, gx, gy, gz);
 }
 
 // Stellar density MN + T3 + V4 (potentials.py:29-49, dehnen_bar.py:1425-1438, 1526-1543).
@@ -462,7 +563,7 @@ __device__ __forceinline__ T phi_only(const PotT<T> &P, T x, T y, T z) {
 
 // true when both Dehnen slots hold their default models
 inline bool canonical_types(const smx_potential &p) {
-    return (p.bar_type == 0 || p.bar_type == 3) && (p.bulge_type == 0 || p.bulge_type == 14);
+    return (p.bar_type == 0 || p.bar_type == 3) && (p.bulge_type == 0 || p.bulge_type == 14) && p.cyl_n_modes == 0;
 }
 
 }  // namespace smx

@@ -19,43 +19,57 @@ constexpr int GJ_B = 64;      // elimination block
 constexpr int GJ_T = 128;     // update tile
 
 // unblocked Gauss-Jordan of the 64 x 64 diagonal block k (column-major, leading
-// dimension ld), P written column-major 64 x 64
+// dimension ld), P written column-major 64 x 64.  256 threads on a 16 x 16 grid, each
+// holding a 4 x 4 tile in registers (the pivot loop is unrolled, so every register
+// index is static); per pivot the 16 threads on the pivot row and the 16 on the pivot
+// column publish their parts through shared memory (double-buffered, one barrier per
+// pivot).  Every update is s_rc - s_rk (s_kc / s_kk), in the order of the textbook form.
 __global__ void __launch_bounds__(256) gj_diag_kernel(const float *__restrict__ A, int64_t ld, int64_t k0, float *P,
                                                       int *flag) {
-    __shared__ float s[GJ_B][GJ_B + 1];   // s[row][col]
-    for (int e = threadIdx.x; e < GJ_B * GJ_B; e += blockDim.x) {
-        const int r = e % GJ_B, c = e / GJ_B;
-        s[r][c] = A[(k0 + r) + ld * (k0 + c)];
-    }
-    __syncthreads();
-    constexpr int PER = GJ_B * GJ_B / 256;
+    __shared__ float rowb[2][GJ_B], colb[2][GJ_B];
+    const int tr = threadIdx.x / 16, tc = threadIdx.x % 16;
+    float a[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) a[i][j] = A[(k0 + 4 * tr + i) + ld * (k0 + 4 * tc + j)];
+#pragma unroll
     for (int k = 0; k < GJ_B; ++k) {
-        const float piv = s[k][k];
-        if (!(piv > 0.0f)) {
+        const int b = k & 1, kb = k >> 2, kr = k & 3;
+        if (tr == kb) {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) rowb[b][4 * tc + j] = a[kr][j];
+        }
+        if (tc == kb) {
+#pragma unroll
+            for (int i = 0; i < 4; ++i) colb[b][4 * tr + i] = a[i][kr];
+        }
+        __syncthreads();
+        const float piv = rowb[b][k];
+        if (!(piv > 0.0f)) {   // uniform: every thread read the same pivot
             if (threadIdx.x == 0) atomicExch(flag, 1);
-            return;   // uniform: every thread read the same pivot
+            return;
         }
         const float ip = 1.0f / piv;
-        float nv[PER];
 #pragma unroll
-        for (int q = 0; q < PER; ++q) {
-            const int e = threadIdx.x + q * 256;
-            const int r = e % GJ_B, c = e / GJ_B;
-            float v;
-            if (r == k) v = (c == k) ? ip : s[k][c] * ip;
-            else if (c == k) v = -s[r][k] * ip;
-            else v = s[r][c] - s[r][k] * (s[k][c] * ip);
-            nv[q] = v;
-        }
-        __syncthreads();
+        for (int i = 0; i < 4; ++i) {
+            const int r = 4 * tr + i;
 #pragma unroll
-        for (int q = 0; q < PER; ++q) {
-            const int e = threadIdx.x + q * 256;
-            s[e % GJ_B][e / GJ_B] = nv[q];
+            for (int j = 0; j < 4; ++j) {
+                const int c = 4 * tc + j;
+                float v;
+                if (r == k) v = (c == k) ? ip : rowb[b][c] * ip;
+                else if (c == k) v = -colb[b][r] * ip;
+                else v = a[i][j] - colb[b][r] * (rowb[b][c] * ip);
+                a[i][j] = v;
+            }
         }
-        __syncthreads();
+        // the next pivot writes the other buffers, so one barrier per pivot suffices
     }
-    for (int e = threadIdx.x; e < GJ_B * GJ_B; e += blockDim.x) P[e] = s[e % GJ_B][e / GJ_B];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) P[(4 * tr + i) + GJ_B * (4 * tc + j)] = a[i][j];
 }
 
 // R (64 x mp, row r at R + mp r) = P A[k block rows, :]; grid over 128-column tiles

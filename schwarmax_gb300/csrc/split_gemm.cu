@@ -550,8 +550,9 @@ int gemm(const Operand &A, const Operand &B, const Acc &acc, bool lower_only, in
         return launch_gemm<4, 5, 6, 112, 3>(A, B, acc, lower_only, err, s, skip);
     if (B.tile_rows == 112 && key == 45 && lmax == 5)
         return launch_gemm<4, 5, 5, 112, 3>(A, B, acc, lower_only, err, s, skip);
+    if (B.tile_rows == 128 && key == 54 && lmax == 6)
+        return launch_gemm<5, 4, 6, 128, 3>(A, B, acc, lower_only, err, s, skip);
     if (lmax != 0) return set_error(SMX_ERR_UNSUPPORTED, "split gemm: no kernel with pairs up to s + t = %d", lmax);
-    if (B.tile_rows == 96 && key == 33) return launch_gemm<3, 3, 6, 96, 3>(A, B, acc, lower_only, err, s, skip);
     if (B.tile_rows == 112) {
         switch (key) {
             case 22: return launch_gemm<2, 2, 4, 112, 2>(A, B, acc, lower_only, err, s, skip);
@@ -564,7 +565,6 @@ int gemm(const Operand &A, const Operand &B, const Acc &acc, bool lower_only, in
         }
     } else if (B.tile_rows == 128) {
         switch (key) {
-            case 33: return launch_gemm<3, 3, 6, 128, 3>(A, B, acc, lower_only, err, s, skip);
             case 44: return launch_gemm<4, 4, 8, 128, 3>(A, B, acc, lower_only, err, s, skip);
             case 54: return launch_gemm<5, 4, 9, 128, 3>(A, B, acc, lower_only, err, s, skip);
             case 55: return launch_gemm<5, 5, 10, 128, 3>(A, B, acc, lower_only, err, s, skip);

@@ -131,14 +131,15 @@ struct Acc {
 int exact_levels(const Operand &A, const Operand &B);
 
 // Launch C += A B^T (A: M x K, B: N x K) into acc.  Supported: 4 or 5 slices
-// per operand and 2 x 2 or 3 x 3 with B.tile_rows 112, 3 x 3, 4 x 4, 5 x 4 or 5 x 5
-// with 128, 5 x 5 with 64, 3 x 3 or 7 x 7 with 96.  An operand stored with more slices can be
+// per operand and 2 x 2 or 3 x 3 with B.tile_rows 112, 4 x 4, 5 x 4 or 5 x 5 with
+// 128, 5 x 5 with 64, 7 x 7 with 96.  An operand stored with more slices can be
 // passed with a smaller S: its leading slices are the value rounded to 8 S - 1 bits.
 // lower_only: only output tiles with column tile <= row tile (symmetric results,
 // requires A.tile_rows == B.tile_rows).  err receives a nonzero code if a wait
 // in the kernel gave up.
-// lmax = 0 forms every slice pair; lmax = 5, 6 or 7 (4 x 5 slices, 112-wide tiles)
-// drops the pairs s + t > lmax, about 2^-8(lmax-1) of max|A| max|B| per product term.
+// lmax = 0 forms every slice pair; lmax = 5, 6 or 7 (4 x 5 slices, 112-wide tiles) or
+// 6 (5 x 4 slices, 128-wide tiles) drops the pairs s + t > lmax, about 2^-8(lmax-1) of
+// max|A| max|B| per product term.
 // skip (optional device flag): when *skip != 0 at run time the launched kernels
 // return at once (a step of an iteration that has converged on the device).
 int gemm(const Operand &A, const Operand &B, const Acc &acc, bool lower_only, int *err, cudaStream_t s,

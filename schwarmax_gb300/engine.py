@@ -44,6 +44,9 @@ class Settings:
     order_probe: bool = False        # sampled mode: order the orbits by the cost of a one-period probe
     nnls: str = None                 # "mixed" / "fp64" NNLS independently of the orbits (None: follow precision)
     autotune: bool = False           # batched evaluations: tuned integrator launch (autotune.py, cached)
+    bootstrap: str = "gaussian"      # "gaussian": the reference's perturbed data rows (likelihood.py:199-211);
+                                     # "poisson": Poisson(1) weights of the apertures per resample (one solve each)
+    bootstrap_seed: int = 0          # seed of the Poisson weights
 
     @property
     def dtype(self):
@@ -321,6 +324,40 @@ def evaluate(pot, params_disk_rho, dd: DeviceData, grid: Grid, st: Settings, nnl
     return r
 
 
+def poisson_weights(n_boot, n_bins, seed=0):
+    """Poisson(1) weight of every aperture in every resample, (n_boot, n_bins) double."""
+    rng = np.random.default_rng(seed)
+    return torch.as_tensor(rng.poisson(1.0, (n_boot, n_bins)).astype(np.float64), device="cuda")
+
+
+def solve_library_poisson(d, dd: DeviceData, nc, lib, st: Settings, nnls_maxiter, regularization, weights,
+                          sigma_amplify, w_init, lum):
+    """The Poisson bootstrap: resample b weighs aperture g by k_bg ~ Poisson(1), so its
+    design and data rows (xy, h1..h4 of g) are scaled by sqrt(k_bg) and it is solved on
+    its own (the design differs per resample), against the unperturbed data; its chi^2
+    weighs the aperture terms by k_bg (likelihood.py:214-226 with weights).  Returns
+    (W (B, n), maps, logl (B,))."""
+    nb = dd.n_bins
+    B = dd.n_boot
+    row_scale, Y0 = nnls_inputs(d, dd, nc, weights, boot=False)
+    K = poisson_weights(B, nb, st.bootstrap_seed)
+    rows_k = torch.cat([torch.ones(B, nc, dtype=torch.float64, device="cuda")] + [K] * 5, dim=1).sqrt()
+    rm = row_map(nc, nb)
+    W = torch.stack([kernels.nnls_admm(lib, rm, (row_scale * rows_k[b]).contiguous(),
+                                       (Y0[0] * rows_k[b])[None].contiguous(), nnls_maxiter, regularization, w_init,
+                                       mixed=st.nnls_mixed)[0] for b in range(B)])
+    y_xy_b, y_h_b, sh_raw = likelihood_data(dd)
+    maps, _ = kernels.model_maps(lib, nc, nb, W, d["gamma"].contiguous(), dd.v0, dd.s, d["y_rz"].contiguous(), dd.xy,
+                                 y_xy_b, y_h_b, sh_raw, lum, sigma_amplify, want_maps=True)
+    m = split_maps(maps, nc, nb)
+    amp = sigma_amplify
+    res = torch.nansum(((m["density_3d_model"] - d["y_rz"]) / (0.1 * d["y_rz"] * amp)) ** 2)
+    res = res + (K * ((m["surface_density"] - dd.xy) / (0.1 * dd.xy * amp)) ** 2).nansum(dim=1)
+    for k in range(4):
+        res = res + (K * ((m[f"h{k + 1}"] - dd.h[k]) / (sh_raw[k] * amp)) ** 2).nansum(dim=1)
+    return W, maps, -0.5 * res
+
+
 def solve_library(pot, params_disk_rho, dd: DeviceData, grid: Grid, st: Settings, lib, nnls_maxiter=200,
                   regularization=1.0, weights=(math.sqrt(5.0), math.sqrt(5.0), 1.0), sigma_amplify=1.0,
                   want_maps=True):
@@ -332,6 +369,13 @@ def solve_library(pot, params_disk_rho, dd: DeviceData, grid: Grid, st: Settings
     y_rz_raw = kernels.density_target(pot, st.dtype, dd.R_grid, dd.z_grid, dd.phi_grid, dd.dR, dd.dz, dd.dphi,
                                       dd.sample)
     d = data_terms(dd, params_disk_rho, y_rz_raw, n)
+    if st.bootstrap == "poisson":
+        host = torch.stack([d["y_rz"].sum() / n, d["mmpo"]]).cpu()
+        W, maps, logl = solve_library_poisson(d, dd, nc, lib, st, nnls_maxiter, regularization, weights,
+                                              sigma_amplify, float(host[0]), float(host[1]) * d["l2m"])
+        return dict(data=d, W=W, maps=maps if want_maps else None, logl=logl, n_cells=nc, n_bins=nb)
+    if st.bootstrap != "gaussian":
+        raise ValueError(f"unknown bootstrap {st.bootstrap!r} (gaussian or poisson)")
     row_scale, Y = nnls_inputs(d, dd, nc, weights)
     # w = z = sum(y_Rzphi)/n at the start (nnls.py:122); read back with mmpo in one copy
     host = torch.stack([d["y_rz"].sum() / n, d["mmpo"]]).cpu()

@@ -36,11 +36,54 @@ def _type_code(t, default):
     return int(t)
 
 
-def potential_struct(params_baryon, params_halo, bulge_mass=None, bar_type=None, bulge_type=None):
+class CylSplineTable:
+    """A cylindrical-spline potential table (CylindricalSpline.py:270-352, the dictionary
+    get_phi_m returns: Rgrid, Zgrid, R0, m, Phi_m_real, Phi_m_img, Mx_real, My_real,
+    Mx_img, My_img) in device memory, for the smx_potential fields cyl_*.  The modes must
+    be m = 0, 1, .., M in order, as get_phi_m makes them."""
+
+    KEYS = ("Phi_m_real", "Phi_m_img", "Mx_real", "My_real", "Mx_img", "My_img")
+
+    def __init__(self, dict_phi_m):
+        import numpy as np
+        d = {k: np.asarray(dict_phi_m[k].cpu() if isinstance(dict_phi_m[k], torch.Tensor) else dict_phi_m[k])
+             for k in ("Rgrid", "Zgrid", "R0", "m") + self.KEYS}
+        m = d["m"].astype(int).reshape(-1)
+        if not np.array_equal(m, np.arange(len(m))):
+            raise NotImplementedError("cylindrical spline modes must be m = 0, 1, .., M (get_phi_m's order)")
+        nr, nz = len(d["Rgrid"]), len(d["Zgrid"])
+        coef = np.stack([d[k][:len(m)] for k in self.KEYS], axis=1)          # (modes, 6, nr, nz)
+        if coef.shape != (len(m), 6, nr, nz):
+            raise ValueError(f"cylindrical spline table of shape {coef.shape}, expected {(len(m), 6, nr, nz)}")
+        self.r0 = float(d["R0"].reshape(-1)[0])
+        self.r = torch.as_tensor(d["Rgrid"], dtype=torch.float64, device="cuda").contiguous()
+        self.z = torch.as_tensor(d["Zgrid"], dtype=torch.float64, device="cuda").contiguous()
+        self.coef = torch.as_tensor(coef, dtype=torch.float64, device="cuda").contiguous()
+        self.n_modes, self.n_r, self.n_z = len(m), nr, nz
+
+    def attach(self, pot):
+        pot.cyl_n_r, pot.cyl_n_z, pot.cyl_n_modes, pot.cyl_r0 = self.n_r, self.n_z, self.n_modes, self.r0
+        pot.cyl_r_grid, pot.cyl_z_grid, pot.cyl_coef = self.r.data_ptr(), self.z.data_ptr(), self.coef.data_ptr()
+        pot._cyl = self            # keeps the device table alive with the struct
+        return pot
+
+
+def cylspline_only(table):
+    """smx_potential holding the cylindrical-spline component alone (the analytic ones
+    at zero mass)."""
+    pot = SmxPotential(halo_M=0.0, halo_Rs=1.0, halo_qa=1.0, halo_qb=1.0, halo_qc=1.0, disc_M=0.0, disc_a=1.0,
+                       disc_b=0.3, bar_M=0.0, bar_a=0.8, bar_b=0.3, bar_L=4.0, bar_gamma=GAMMA_BAR, bulge_M=0.0,
+                       bulge_a=V4_A, bulge_b=V4_B, bulge_L=V4_L, bulge_gamma=V4_GAMMA)
+    t = table if isinstance(table, CylSplineTable) else CylSplineTable(table)
+    return t.attach(pot)
+
+
+def potential_struct(params_baryon, params_halo, bulge_mass=None, bar_type=None, bulge_type=None, cylspline=None):
     """Reference parameter dicts -> smx_potential.  Shifted or tilted components
     (potentials.py:8-15) are not part of the canonical model.  bar_type / bulge_type
     ("T1".."T4", "V1".."V4", default T3 / V4) choose another Dehnen & Aly model
-    (dehnen_bar.py:1272-1555) for either slot."""
+    (dehnen_bar.py:1272-1555) for either slot.  cylspline (a CylSplineTable or
+    get_phi_m's dictionary) adds a cylindrical-spline component to the potential."""
     for p in (params_baryon, params_halo):
         for k in ("x_origin", "y_origin", "z_origin", "dirx", "diry"):
             if k in p and float(p[k]) != 0.0:
@@ -48,7 +91,7 @@ def potential_struct(params_baryon, params_halo, bulge_mass=None, bar_type=None,
         if "dirz" in p and float(p["dirz"]) <= 0.0:
             raise NotImplementedError("the symmetry axis must be +z")
     m_bar = 10.0 ** float(params_baryon["logM_bar"])
-    return SmxPotential(
+    pot = SmxPotential(
         halo_M=10.0 ** float(params_halo["logM"]), halo_Rs=float(params_halo["Rs"]),
         halo_qa=float(params_halo.get("a", 1.0)), halo_qb=float(params_halo.get("b", 1.0)),
         halo_qc=float(params_halo.get("c", 1.0)),
@@ -58,6 +101,9 @@ def potential_struct(params_baryon, params_halo, bulge_mass=None, bar_type=None,
         bar_L=float(params_baryon["L_bar"]), bar_gamma=GAMMA_BAR,
         bulge_M=m_bar if bulge_mass is None else float(bulge_mass), bulge_a=V4_A, bulge_b=V4_B, bulge_L=V4_L,
         bulge_gamma=V4_GAMMA, bar_type=_type_code(bar_type, 3), bulge_type=_type_code(bulge_type, 14))
+    if cylspline is not None:
+        (cylspline if isinstance(cylspline, CylSplineTable) else CylSplineTable(cylspline)).attach(pot)
+    return pot
 
 
 class _Canonical:

@@ -45,3 +45,45 @@ def where(c, x=None, y=None):
 def take_jax(a, idx):
     idx = _np.asarray(idx)
     return _np.asarray(a)[_np.where(idx < 0, idx + len(a), idx)]
+
+
+class _AtIndex:
+    def __init__(self, arr, idx):
+        self.arr, self.idx = arr, idx
+
+    def set(self, v):
+        out = _np.array(self.arr, copy=True).view(JArray)
+        out[self.idx] = v
+        return out
+
+    def add(self, v):
+        out = _np.array(self.arr, copy=True).view(JArray)
+        out[self.idx] += v
+        return out
+
+    def get(self):
+        return _np.asarray(self.arr)[self.idx]
+
+
+class _At:
+    def __init__(self, arr):
+        self.arr = arr
+
+    def __getitem__(self, idx):
+        return _AtIndex(self.arr, idx)
+
+
+class JArray(_np.ndarray):
+    """An ndarray with JAX's functional update syntax, x.at[idx].set(v) / .add(v)."""
+
+    @property
+    def at(self):
+        return _At(self)
+
+
+def zeros(shape, dtype=None):
+    return _np.zeros(shape, dtype=dtype if dtype is not None else _np.float64).view(JArray)
+
+
+def zeros_like(a, dtype=None):
+    return _np.zeros_like(_np.asarray(a), dtype=dtype).view(JArray)

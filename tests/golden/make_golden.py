@@ -461,6 +461,51 @@ def case_analysis():
          psf_grid_res=np.array(150), psf_P=P)
 
 
+def case_cylspline():
+    """evaluate_phi and get_acc (CylindricalSpline.py:354-519) on a table in the format
+    of get_phi_m (CylindricalSpline.py:270-352): the azimuthal modes m = 0..4 of the
+    canonical potential on get_phi_m's (R, z) grid (R geometric in [0.01, 30], z = 0 and
+    geometric in [0.01, 10], R0 = R[NR // 2], both in asinh(./R0)), with the second
+    derivatives from the reference's own jax_precompute_splines (CubicSpline.py:55-97),
+    evaluated at 160 points inside and 8 outside the grid."""
+    import CubicSpline as cub
+    import CylindricalSpline as cs
+    pb, ph = params_pair()
+    NR, NZ, Mmax, Nphi = 24, 16, 4, 32
+    R = np.geomspace(1e-2, 30.0, NR)
+    Z = np.concatenate([[0.0], np.geomspace(1e-2, 10.0, NZ)])
+    R0 = R[NR // 2]
+    Rt, Zt = np.arcsinh(R / R0), np.arcsinh(Z / R0)
+    ang = np.linspace(0.0, 2 * np.pi, Nphi, endpoint=False)
+    Rg, Zg, Ag = np.meshgrid(R, Z, ang, indexing="ij")
+    Phi = np.asarray(likelihood.potential_func((Rg * np.cos(Ag)).ravel(), (Rg * np.sin(Ag)).ravel(), Zg.ravel(),
+                                               pb, ph)).reshape(Rg.shape)
+    modes = np.fft.fft(Phi, axis=2)[..., :Mmax + 1] / Nphi          # Phi_m = mean of Phi e^{-i m phi}
+    tab = {k: np.zeros((Mmax + 1, NR, NZ + 1)) for k in ("Phi_m_real", "Phi_m_img", "Mx_real", "My_real",
+                                                         "Mx_img", "My_img")}
+    for m in range(Mmax + 1):
+        for part, vals in (("real", modes[..., m].real), ("img", modes[..., m].imag)):
+            tab[f"Phi_m_{part}"][m] = vals
+            Mx, My = cub.jax_precompute_splines((Rt, Zt), vals)
+            tab[f"Mx_{part}"][m] = np.asarray(Mx)
+            tab[f"My_{part}"][m] = np.asarray(My)
+    d = dict(Rgrid=Rt, Zgrid=Zt, R0=np.array([R0]), m=np.arange(Mmax + 1), **tab)
+    rng = np.random.default_rng(11)
+    n = 160
+    Rq = np.exp(rng.uniform(np.log(0.02), np.log(25.0), n))
+    aq = rng.uniform(-np.pi, np.pi, n)
+    zq = rng.uniform(-8.0, 8.0, n) * rng.uniform(0, 1, n) ** 2
+    x, y = Rq * np.cos(aq), Rq * np.sin(aq)
+    x[:4], y[:4], zq[:4] = [3.0, 0.0, -2.0, 1e-3], [0.0, 2.5, -2.0, 0.0], [0.0, 0.0, -1.5, 0.3]
+    # outside the grid: fill value 0 for Phi and its derivatives
+    x = np.concatenate([x, [40.0, 0.0, -35.0, 5.0, 0.0, 3.0, 20.0, -1.0]])
+    y = np.concatenate([y, [0.0, 45.0, 10.0, 1.0, 0.0, 0.0, 25.0, 0.5]])
+    zq = np.concatenate([zq, [0.0, 1.0, -2.0, 12.0, -15.0, 11.0, 0.0, -10.5]])
+    phi = np.asarray(cs.evaluate_phi(x, y, zq, d))
+    acc = np.asarray(cs.get_acc(x, y, zq, d))
+    save("cylspline", x=x, y=y, z=zq, phi=phi, acc=acc, params=flat_params(pb, ph), **d)
+
+
 if __name__ == "__main__":
     print("G =", constants.G, "KPCGYR_TO_KMS =", constants.KPCGYR_TO_KMS)
     cases = sys.argv[2:] or ["potential", "small_funcs", "jeans", "integrate", "nnls", "end_to_end", "with_orbit",

@@ -140,3 +140,46 @@ def test_noncanonical_model_rejected(smx):
     bad = dict(bary, x_origin=1.0)
     with pytest.raises(NotImplementedError):
         smx.build_model(smx.density_func, smx.potential_func, halo, bad, dd, 4, 48, **_grid_kw(dd))
+
+
+def test_poisson_bootstrap_matches_oracle(smx):
+    """The Poisson-weighted bootstrap (config 1's resampling: aperture g of resample b
+    weighted by k_bg ~ Poisson(1)), FP64: every resample's weights against the oracle's
+    Cholesky ADMM on the row-scaled design, and its weighted chi^2 (likelihood.py:214-226
+    with the weights) against NumPy on the oracle's model maps."""
+    from oracle import model as omodel, nnls as onnls
+    from schwarmax_gb300 import engine
+    from schwarmax_gb300.likelihood import log_likelihoods
+    g = golden("end_to_end")
+    dd = tiny_dict_data(g)
+    amp = float(g["sigma_amplify"])
+    logl, r = log_likelihoods(g["theta"], dd, 4, 48, sigma_amplify=amp,
+                              settings=dict(precision="fp64", bootstrap="poisson"))
+    ddv = engine.device_data(dd)
+    lib = r["lib"]["library"].cpu().numpy()
+    d = r["data"]
+    nc, nb, B = 48, 4, ddv.n_boot
+    row_scale, Y0 = engine.nnls_inputs(d, ddv, nc, (np.sqrt(5.0), np.sqrt(5.0), 1.0), boot=False)
+    rm = engine.row_map(nc, nb).cpu().numpy()
+    U = (lib[:, rm] * row_scale.cpu().numpy()[None]).T
+    K = engine.poisson_weights(B, nb, 0).cpu().numpy()
+    w_init = float((d["y_rz"].sum() / lib.shape[0]).item())
+    Z = []
+    for b in range(B):
+        sq = np.sqrt(np.concatenate([np.ones(nc)] + [K[b]] * 5))
+        Z.append(onnls.admm(U * sq[:, None], (Y0.cpu().numpy()[0] * sq)[None], w_init, 1.0, 200)[0])
+    Z = np.array(Z)
+    W = r["W"].cpu().numpy()
+    np.testing.assert_allclose(W, Z, rtol=0, atol=1e-9 * np.abs(Z).max())
+    cols = lambda a, b_: lib[:, a:b_].T          # noqa: E731
+    lum = float(d["mmpo"].item()) * float(d["l2m"])
+    d3, d2, h1, h2, h3, h4, _, _ = omodel.compute_model_batch(
+        Z, cols(0, nc), cols(nc, nc + nb), *[cols(nc + (1 + k) * nb, nc + (2 + k) * nb) for k in range(1, 5)],
+        d["gamma"].cpu().numpy(), ddv.v0.cpu().numpy(), ddv.s.cpu().numpy())
+    y_rz, xy = d["y_rz"].cpu().numpy(), ddv.xy.cpu().numpy()
+    sh = (ddv.h_err + 1e-12).cpu().numpy()
+    hd = ddv.h.cpu().numpy()
+    res = np.nansum(((d3 - y_rz) / (0.1 * y_rz * amp)) ** 2) + np.nansum(K * ((d2 * lum - xy) / (0.1 * xy * amp)) ** 2, 1)
+    for k, hk in enumerate((h1, h2, h3, h4)):
+        res = res + np.nansum(K * ((hk - hd[k]) / (sh[k] * amp)) ** 2, 1)
+    np.testing.assert_allclose(logl.cpu().numpy(), -0.5 * res, rtol=1e-9)

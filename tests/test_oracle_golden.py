@@ -227,3 +227,19 @@ def test_dehnen_models_match_reference(name):
     p = op.DEHNEN_PHI[code](X, Y, Z, M, a, b, L, gam)
     acc = -np.stack([p.d[0], p.d[1], p.d[2]], -1)
     np.testing.assert_allclose(acc, g[name + "_acc"], rtol=1e-9, atol=1e-10 * np.abs(g[name + "_acc"]).max())
+
+
+def test_cylspline_matches_reference():
+    """The cylindrical-spline potential (CylindricalSpline.py:354-519, CubicSpline.py:5-305):
+    Phi and -grad Phi of a table in get_phi_m's format, and the table's spline second
+    derivatives, against the reference's own evaluate_phi / get_acc / jax_precompute_splines."""
+    from oracle import cylspline as oc
+    g = dict(golden("cylspline"))
+    phi, acc = oc.phi_and_acc(g["x"], g["y"], g["z"], g)
+    np.testing.assert_allclose(phi, g["phi"], rtol=0, atol=1e-13 * np.abs(g["phi"]).max())
+    np.testing.assert_allclose(acc, g["acc"], rtol=0, atol=1e-13 * np.abs(g["acc"]).max())
+    for m in g["m"]:
+        for part in ("real", "img"):
+            Mx, My = oc.precompute_splines(g["Rgrid"], g["Zgrid"], g[f"Phi_m_{part}"][m])
+            np.testing.assert_allclose(Mx, g[f"Mx_{part}"][m], rtol=1e-12, atol=1e-12 * np.abs(Mx).max())
+            np.testing.assert_allclose(My, g[f"My_{part}"][m], rtol=1e-12, atol=1e-12 * np.abs(My).max())
