@@ -366,6 +366,17 @@ int smx_spd_inverse_f32_workspace_size(int64_t m, size_t *bytes);
 int smx_spd_inverse_f32(const double *G, int64_t m, float *Xinv, void *workspace, size_t workspace_bytes,
                         void *stream);
 
+/* The seed the mixed NNLS actually refines: G^-1 (double, exactly symmetric) of FP32
+ * quality by block elimination on Schur complements, G = [A B; B^T C] ->
+ * [A^-1 + V W^T, -V; -V^T, S^-1] with W = A^-1 B, S = C - B^T W, V = W S^-1, recursing
+ * on A and S down to blocks of 1,024 rows (inverted by the Gauss-Jordan above); the
+ * products run on the split tensor-core kernel (4 slices, pairs s + t <= 5).  About
+ * m^3 tensor flops per slice pair instead of 2 m^3 FP32 flops.  Returns SMX_ERR_NUMERIC
+ * when a pivot is not positive.  Synchronises the stream. */
+int smx_spd_inverse_seed_workspace_size(int64_t m, size_t *bytes);
+int smx_spd_inverse_seed(const double *G, int64_t m, double *X, void *workspace, size_t workspace_bytes,
+                         void *stream);
+
 /* ------------------------------------------------------- model maps, chi2 */
 typedef struct {
     int64_t n;           /* orbits */

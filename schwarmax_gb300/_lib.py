@@ -34,7 +34,8 @@ EXPORTS = ["smx_version", "smx_kernel_launches", "smx_status_string", "smx_last_
            "smx_nnls_admm", "smx_nnls_jackknife_workspace_size", "smx_nnls_jackknife", "smx_split_gemm_workspace_size",
            "smx_split_gemm", "smx_model_maps", "smx_model_maps_workspace_size", "smx_lcirc_table", "smx_spline_eval",
            "smx_circularity", "smx_histogram2d", "smx_psf_transfer_workspace_size", "smx_psf_transfer",
-           "smx_rmh_propose", "smx_rmh_accept", "smx_spd_inverse_f32_workspace_size", "smx_spd_inverse_f32"]
+           "smx_rmh_propose", "smx_rmh_accept", "smx_spd_inverse_f32_workspace_size", "smx_spd_inverse_f32",
+           "smx_spd_inverse_seed_workspace_size", "smx_spd_inverse_seed"]
 
 
 class SmxError(RuntimeError):

@@ -46,8 +46,6 @@ namespace smx {
 // FP32 SPD inverse by blocked Gauss-Jordan (spd_inverse.cu)
 int64_t spd_inverse_padded(int64_t m);
 size_t spd_inverse_workspace(int64_t m);
-int spd_inverse_inplace(float *Ap, int64_t mp, float *ws, int *flag, cudaStream_t s);
-__global__ void gj_pad_kernel(const double *__restrict__ G, int64_t m, float *Ap, int64_t mp);
 
 struct Handles {
     cublasHandle_t blas = nullptr;
@@ -93,7 +91,7 @@ static inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 // sliced operands of the split path (tile geometry only; pointers are set in run)
 struct SplitShapes {
     split::Operand Ua, Ut, Xg, Ds, Es, Fs;   // Xg: G^-1 for the iterations
-    split::Operand G7, X7, X5, R5;           // Newton-Schulz operands
+    split::Operand G7, X7, X4, R4;           // Newton-Schulz operands
 };
 
 static SplitShapes split_shapes(const smx_nnls_problem *p) {
@@ -108,8 +106,8 @@ static SplitShapes split_shapes(const smx_nnls_problem *p) {
     sh.Fs = split::make_operand(B, m, vt, 5);
     sh.G7 = split::make_operand(m, m, split::MT, 7);
     sh.X7 = split::make_operand(m, m, 96, 7);
-    sh.X5 = split::make_operand(m, m, split::MT, 5);
-    sh.R5 = split::make_operand(m, m, split::MT, 5);
+    sh.X4 = split::make_operand(m, m, split::MT, 4);
+    sh.R4 = split::make_operand(m, m, split::MT, 4);
     return sh;
 }
 
@@ -118,7 +116,7 @@ struct Layout {
     // split path
     size_t Tacc, Racc, rowmax, err;
     size_t Ua, Ua_e, Ut, Ut_e, Xg, Xg_e, Ds, Ds_e, Es, Es_e, Fs, Fs_e;
-    size_t G7, G7_e, X7, X7_e, X5, X5_e, R5, R5_e, Gf, gjws, nsflag, Xd, Rd, Ebuf, Fbuf, gdiag, colmax;
+    size_t G7, G7_e, X7, X7_e, X4, X4_e, R4, R4_e, Gf, gjws, nsflag, Xd, Rd, Ebuf, Fbuf, gdiag, colmax;
     int lwork_s;   // float Cholesky / inverse scratch (floats)
     int64_t acc_elems;
     size_t work_bytes, host_bytes;   // device / host scratch of the factorisation and inversion
@@ -177,11 +175,13 @@ static int layout(const smx_nnls_problem *p, Layout *L, cusolverDnHandle_t solve
         op(sh.Fs, L->Fs, L->Fs_e);
         op(sh.G7, L->G7, L->G7_e);
         op(sh.X7, L->X7, L->X7_e);
-        op(sh.X5, L->X5, L->X5_e);
-        op(sh.R5, L->R5, L->R5_e);
-        const int64_t mp = spd_inverse_padded((int64_t)m);
-        L->Gf = take((size_t)mp * mp * sizeof(float));      // padded float copy of G, inverted in place
-        L->gjws = take(spd_inverse_workspace((int64_t)m));
+        op(sh.X4, L->X4, L->X4_e);
+        op(sh.R4, L->R4, L->R4_e);
+        // the seed's Gauss-Jordan blocks (at most kSeedBaseRows rows)
+        const int64_t mb = (int64_t)m < kSeedBaseRows ? (int64_t)m : kSeedBaseRows;
+        const int64_t mp = spd_inverse_padded(mb);
+        L->Gf = take((size_t)mp * mp * sizeof(float));
+        L->gjws = take(spd_inverse_workspace(mb));
         L->nsflag = take(16 * sizeof(int));
         L->Xd = take(m * m * sizeof(double));
         L->Rd = take(m * m * sizeof(double));
@@ -298,6 +298,9 @@ __device__ __forceinline__ double product_value(const unsigned long long *T, con
 enum { COL_INIT = 0, COL_RESID = 1, COL_PLAIN = 2, COL_UPDATE = 3 };
 
 constexpr int kNsMaxSteps = 5;   // Newton-Schulz steps at most (a seed residual of 0.2 needs 4)
+constexpr double kNsStopResidual2 = 1e-8;   // ||R||_F^2 of the input of the last step
+constexpr int kNsResidualLevels = 7;   // slice pairs s + t <= 7 of the residual G X (7 x 7 slices)
+constexpr int kNsUpdateLevels = 5;     // slice pairs s + t <= 5 of the update X R (4 x 4 slices)
 
 constexpr int VS = 5;          // slices of the vector operands: 39 bits below each column's largest magnitude
 // Slice pairs (s, t) of the skinny products U D and H^T E with s + t <= kSkinnyLevels.
@@ -478,13 +481,6 @@ __global__ void gram_combine_kernel(unsigned long long *T, float *R, const int32
 
 // Newton-Schulz seed: X0 = the symmetric part of the float inverse (padded, leading
 // dimension mp), in double
-__global__ void seed_kernel(const float *Gp, int64_t mp, double *X, int64_t m) {
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < m * m; k += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t r = k % m, col = k / m;
-        X[k] = 0.5 * ((double)Gp[r + mp * col] + (double)Gp[col + mp * r]);
-    }
-}
-
 // Device-side control of the Newton-Schulz steps (no host read-back): flag[0] = 1
 // while steps are still to run; after the residual of a step, with ss = ||I - G X||_F^2
 // of the step's input: a step whose input is below thr2 is the last one; an input at
@@ -541,15 +537,15 @@ __global__ void ns_residual_kernel(unsigned long long *T, float *Racc, const int
 }
 
 // X <- X + X R.  X R = X - X G X is symmetric, so the product is formed on the lower
-// tiles only (tiles of split::MT rows) and an element of an upper tile takes the value
-// of its mirror; X stays exactly symmetric.  T and R are cleared by a separate pass
-// (a thread may read the mirror of an element another thread is done with).
+// tiles only (tiles of split::MT rows) and every element above the diagonal takes the
+// value of its mirror; X stays exactly symmetric.  T and R are cleared by a separate
+// pass (a thread may read the mirror of an element another thread is done with).
 __global__ void ns_update_kernel(const unsigned long long *T, const float *Racc, const int32_t *eX,
                                  const int32_t *eR, double *X, int64_t m, const int *skip, int t_shift) {
     if (*skip) return;
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < m * m; k += (int64_t)gridDim.x * blockDim.x) {
         int64_t i = k % m, j = k / m;
-        if (j / split::MT > i / split::MT) {
+        if (j > i) {   // (j, i) lies in a lower tile
             const int64_t t = i;
             i = j;
             j = t;
@@ -643,10 +639,10 @@ static int mixed_setup(const smx_nnls_problem *p, const TL *lib, const int32_t *
     sh.G7.expo = (int32_t *)(ws + L.G7_e);
     sh.X7.slices = (__nv_bfloat16 *)(ws + L.X7);
     sh.X7.expo = (int32_t *)(ws + L.X7_e);
-    sh.X5.slices = (__nv_bfloat16 *)(ws + L.X5);
-    sh.X5.expo = (int32_t *)(ws + L.X5_e);
-    sh.R5.slices = (__nv_bfloat16 *)(ws + L.R5);
-    sh.R5.expo = (int32_t *)(ws + L.R5_e);
+    sh.X4.slices = (__nv_bfloat16 *)(ws + L.X4);
+    sh.X4.expo = (int32_t *)(ws + L.X4_e);
+    sh.R4.slices = (__nv_bfloat16 *)(ws + L.R4);
+    sh.R4.expo = (int32_t *)(ws + L.R4_e);
     unsigned long long *Tacc = (unsigned long long *)(ws + L.Tacc);
     float *Racc = (float *)(ws + L.Racc);
     unsigned long long *rowmax = (unsigned long long *)(ws + L.rowmax);
@@ -669,43 +665,60 @@ static int mixed_setup(const smx_nnls_problem *p, const TL *lib, const int32_t *
     if ((st = split::gemm(sh.Ua, sh.Ua, acc, true, derr, s))) return st;
     gram_combine_kernel<<<grid1d(m * m), 256, 0, s>>>(Tacc, Racc, sh.Ua.expo, G, m, frob, lam, (double)n);
     count_launch();
-    // G^-1: an FP32 inverse (blocked Gauss-Jordan) as the seed, then Newton-Schulz steps
+    // G^-1: a seed of FP32 quality (Schur-complement recursion on split products with
+    // FP32 Gauss-Jordan blocks, spd_inverse_seed), then Newton-Schulz steps
     //   R = I - G X (diagonals exact, off-diagonal parts as a 7 x 7 split
     //   product), X <- X + X R.
     // The new X has residual R^2, whose 2-norm is at most ||R||_F^2: steps
-    // continue until a step's input has ||R||_F <= 1e-5, so the result has
-    // ||I - G X|| <= 1e-10 and X a relative error of at most 1e-10 (a float seed
-    // with ||R||_F ~ 2e-3 needs two steps: 2e-3 -> 4e-6 -> 1.6e-11).
+    // continue until a step's input has ||R||_F <= 1e-4, so the result has
+    // ||I - G X|| <= 1e-8 and X a relative error of at most 1e-8, far below the
+    // 2^-31 slicing of U and H in every iteration (a seed with ||R||_F ~ 5e-3 needs
+    // two steps: 5e-3 -> 3e-5 -> 1e-9).
     // The stopping rule runs on the device (ns_gate_kernel): the kernels of a step
     // that is not needed return at once, and nothing is read back here.
-    const int64_t mp = spd_inverse_padded(m);
     int *nsf = (int *)(ws + L.nsflag);
-    gj_pad_kernel<<<4864, 256, 0, s>>>(G, m, Gp, mp);
-    count_launch();
-    if ((st = spd_inverse_inplace(Gp, mp, (float *)(ws + L.gjws), dinfo + 1, s))) return st;
-    seed_kernel<<<grid1d(m * m), 256, 0, s>>>(Gp, mp, Xd, m);
-    count_launch();
+    {
+        // the slice buffers of the Newton-Schulz operands, the accumulators and Rd are
+        // free until the first step
+        SeedWorkspace sw;
+        sw.a_slices = sh.G7.slices;
+        sw.a_expo = sh.G7.expo;
+        sw.b_slices = sh.X7.slices;
+        sw.b_expo = sh.X7.expo;
+        sw.T = Tacc;
+        sw.R = Racc;
+        sw.rowmax = rowmax;
+        sw.gp = Gp;
+        sw.gjws = (float *)(ws + L.gjws);
+        sw.err = derr;
+        sw.flag = dinfo + 1;
+        SMX_TRY_CUDA(cudaMemcpyAsync(Xd, G, (size_t)m * m * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        if ((st = spd_inverse_seed(Xd, m, m, Rd, sw, s))) return st;
+    }
     if ((st = split::slice_rows<double>(G, 1, m, sh.G7, rowmax, s, true))) return st;   // O_G
     double *rss = frob + 3;
     ns_init_kernel<<<1, 1, 0, s>>>(nsf);
     count_launch();
     const int *skip = nsf + 3;
     for (int step = 0; step < kNsMaxSteps; ++step) {
-        // Residual products keep 7 slices and updates 5 in every step: a first step with
-        // 3-slice products (its output only needs to be as good as ||R0||^2 ~ 4e-6) left a
-        // residual too large for the second step to be the last, and so cost a third step.
-        const split::Operand &g = sh.G7, &x = sh.X7, &xr = sh.X5, &rr = sh.R5;
+        // Residual products keep 7 slices in every step (a first step with 3-slice products,
+        // whose output only needs to be as good as ||R0||^2 ~ 4e-6, left a residual too
+        // large for the second step to be the last, and so cost a third step), with the
+        // slice pairs s + t <= 7: the pairs left out weigh 2^-48 of max|O_G| max|O_X| per
+        // term.  The update X R only has to be good to a fraction of ||R|| <= 2e-3 of X:
+        // 4 slices and pairs s + t <= 5 (2^-32 per term).
+        const split::Operand &g = sh.G7, &x = sh.X7, &xr = sh.X4, &rr = sh.R4;
         if ((st = split::slice_rows<double>(Xd, m, 1, sh.X7, rowmax, s, true, skip))) return st;   // O_X columns over k
-        if ((st = split::gemm(g, x, acc, false, derr, s, 0, skip))) return st;
+        if ((st = split::gemm(g, x, acc, false, derr, s, kNsResidualLevels, skip))) return st;
         SMX_TRY_CUDA(cudaMemsetAsync(rss, 0, sizeof(double), s));
         ns_residual_kernel<<<grid1d(m * m), 256, 0, s>>>(Tacc, Racc, sh.G7.expo, sh.X7.expo, G, Xd, Rd, m, rss, skip,
                                                          8 * (split::exact_levels(g, x) - 1));
-        ns_gate_kernel<<<1, 1, 0, s>>>(rss, 1e-10, nsf);
+        ns_gate_kernel<<<1, 1, 0, s>>>(rss, kNsStopResidual2, nsf);
         count_launch(2);
-        if ((st = split::slice_rows<double>(Xd, 1, m, sh.X5, rowmax, s, false, skip))) return st;   // X rows over k
-        if ((st = split::slice_rows<double>(Rd, m, 1, sh.R5, rowmax, s, false, skip))) return st;   // R columns over k
-        if ((st = split::gemm(xr, rr, acc, true, derr, s, 0, skip))) return st;
-        ns_update_kernel<<<grid1d(m * m), 256, 0, s>>>(Tacc, Racc, sh.X5.expo, sh.R5.expo, Xd, m, skip,
+        if ((st = split::slice_rows<double>(Xd, 1, m, sh.X4, rowmax, s, false, skip))) return st;   // X rows over k
+        if ((st = split::slice_rows<double>(Rd, m, 1, sh.R4, rowmax, s, false, skip))) return st;   // R columns over k
+        if ((st = split::gemm(xr, rr, acc, true, derr, s, kNsUpdateLevels, skip))) return st;
+        ns_update_kernel<<<grid1d(m * m), 256, 0, s>>>(Tacc, Racc, sh.X4.expo, sh.R4.expo, Xd, m, skip,
                                                        8 * (split::exact_levels(xr, rr) - 1));
         clear_kernel<<<grid1d(m * m), 256, 0, s>>>(Tacc, Racc, m * m);
         ns_skip_kernel<<<1, 1, 0, s>>>(nsf);

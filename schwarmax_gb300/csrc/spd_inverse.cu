@@ -12,6 +12,7 @@
 // which leaves A^-1 after the last block.  2 m^3 flops on the FP32 pipe; the matrix
 // is padded to a multiple of 64 with an identity block.
 #include "smx_internal.cuh"
+#include "split_gemm.cuh"
 
 namespace smx {
 
@@ -212,6 +213,141 @@ int spd_inverse_inplace(float *Ap, int64_t mp, float *ws, int *flag, cudaStream_
     return SMX_OK;
 }
 
+// ------------------------------------------------------------ recursive seed
+// G^-1 of a symmetric positive definite G by block elimination on Schur complements,
+//   G = [A B; B^T C]:  X_A = A^-1,  W = X_A B,  S = C - B^T W,  X_S = S^-1,
+//   V = W X_S,  G^-1 = [X_A + V W^T, -V; -V^T, X_S],
+// with A^-1 and S^-1 by the same rule down to blocks of at most kSeedBaseRows rows, which
+// the FP32 Gauss-Jordan above inverts.  The four products of a level run on the split
+// tensor-core kernel with 4 slices and pairs s + t <= 5 (31 bits of every row's and
+// column's largest magnitude), so the result has the quality of an FP32 inverse; the
+// products are about m^3 flops per slice pair in all.  The Schur complements of an SPD
+// matrix are SPD, so no pivoting is needed.  The result is exactly symmetric (the
+// symmetric products are formed on their lower tiles and mirrored).
+
+namespace {
+
+constexpr int kSeedSlices = 4;
+constexpr int kSeedLevels = 5;        // slice pairs s + t <= 5
+
+__device__ __forceinline__ double exp2i(int p) { return __longlong_as_double((long long)(1023 + p) << 52); }
+
+// out = beta out + alpha C for the product C (M x N) in T, R (leading dimension M, row
+// exponents eA, column exponents eB, T in units of 2^-t_shift).  lower: C symmetric,
+// formed on the lower tiles only; every element above the diagonal takes its mirror's
+// value, so the result is exactly symmetric.
+__global__ void seed_combine_kernel(const unsigned long long *__restrict__ T, const float *__restrict__ R,
+                                    const int32_t *__restrict__ eA, const int32_t *__restrict__ eB, int t_shift,
+                                    int64_t M, int64_t N, double alpha, double beta, double *out, int64_t ldo,
+                                    int lower) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < M * N; k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = k % M, j = k / M;
+        int64_t ti = i, tj = j;
+        if (lower && j > i) {   // (j, i) lies in a lower tile
+            ti = j;
+            tj = i;
+        }
+        const int64_t idx = ti + M * tj;
+        const double c = ((double)(long long)T[idx] * exp2i(-t_shift) + (double)R[idx]) * exp2i(eA[ti] + eB[tj] - 14);
+        double *o = out + i + ldo * j;
+        *o = (beta != 0.0 ? beta * *o : 0.0) + alpha * c;
+    }
+}
+
+__global__ void seed_clear_kernel(unsigned long long *T, float *R, int64_t count) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < count; k += (int64_t)gridDim.x * blockDim.x) {
+        T[k] = 0ull;
+        R[k] = 0.0f;
+    }
+}
+
+// X_12 = -V, X_21 = -V^T (V is m1 x m2 with leading dimension m1)
+__global__ void seed_offdiag_kernel(const double *__restrict__ V, int64_t m1, int64_t m2, double *X, int64_t ld) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < m1 * m2; k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = k % m1, j = k / m1;
+        const double v = -V[k];
+        X[i + ld * (m1 + j)] = v;
+        X[(m1 + j) + ld * i] = v;
+    }
+}
+
+// the m x m block at X (leading dimension ld) as a padded float matrix, identity on the padding
+__global__ void seed_pad_kernel(const double *__restrict__ X, int64_t ld, int64_t m, float *Ap, int64_t mp) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < mp * mp; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = e % mp, c = e / mp;
+        Ap[e] = (r < m && c < m) ? (float)X[r + ld * c] : (r == c ? 1.0f : 0.0f);
+    }
+}
+
+// the block back in double, symmetrised
+__global__ void seed_unpad_kernel(const float *__restrict__ Ap, int64_t mp, double *X, int64_t ld, int64_t m) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < m * m; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = e % m, c = e / m;
+        X[r + ld * c] = 0.5 * ((double)Ap[r + mp * c] + (double)Ap[c + mp * r]);
+    }
+}
+
+inline unsigned seed_grid(int64_t count) {
+    int64_t g = (count + 255) / 256;
+    if (g > 152 * 32) g = 152 * 32;
+    return (unsigned)(g < 1 ? 1 : g);
+}
+
+// out = beta out + alpha A_op B_op^T with A_op(i, k) = a[i asr + k asc] (M x K) and
+// B_op(j, k) = b[j bsr + k bsc] (N x K)
+int seed_product(const SeedWorkspace &w, const double *a, int64_t asr, int64_t asc, const double *b, int64_t bsr,
+                 int64_t bsc, int64_t M, int64_t N, int64_t K, bool lower, double alpha, double beta, double *out,
+                 int64_t ldo, cudaStream_t s) {
+    split::Operand A = split::make_operand(M, K, split::MT, kSeedSlices);
+    split::Operand B = split::make_operand(N, K, split::MT, kSeedSlices);
+    A.slices = w.a_slices;
+    A.expo = w.a_expo;
+    B.slices = w.b_slices;
+    B.expo = w.b_expo;
+    int st;
+    if ((st = split::slice_rows<double>(a, asr, asc, A, w.rowmax, s))) return st;
+    if ((st = split::slice_rows<double>(b, bsr, bsc, B, w.rowmax, s))) return st;
+    split::Acc acc{w.T, w.R, M};
+    if ((st = split::gemm(A, B, acc, lower, w.err, s, kSeedLevels))) return st;
+    seed_combine_kernel<<<seed_grid(M * N), 256, 0, s>>>(w.T, w.R, A.expo, B.expo, 8 * (split::exact_levels(A, B) - 1),
+                                                         M, N, alpha, beta, out, ldo, lower ? 1 : 0);
+    seed_clear_kernel<<<seed_grid(M * N), 256, 0, s>>>(w.T, w.R, M * N);
+    count_launch(2);
+    SMX_TRY_CUDA(cudaGetLastError());
+    return SMX_OK;
+}
+
+}  // namespace
+
+// In place: the m x m block at X (leading dimension ld) holds G on entry and the seed
+// of G^-1 on return.  scratch: the W and V blocks of every level (at most 0.7 m^2 doubles).
+int spd_inverse_seed(double *X, int64_t ld, int64_t m, double *scratch, const SeedWorkspace &w, cudaStream_t s) {
+    int st;
+    if (m <= kSeedBaseRows) {
+        const int64_t mp = spd_inverse_padded(m);
+        seed_pad_kernel<<<seed_grid(mp * mp), 256, 0, s>>>(X, ld, m, w.gp, mp);
+        count_launch();
+        if ((st = spd_inverse_inplace(w.gp, mp, w.gjws, w.flag, s))) return st;
+        seed_unpad_kernel<<<seed_grid(m * m), 256, 0, s>>>(w.gp, mp, X, ld, m);
+        count_launch();
+        SMX_TRY_CUDA(cudaGetLastError());
+        return SMX_OK;
+    }
+    const int64_t m1 = (m / 2 + split::MT - 1) / split::MT * split::MT, m2 = m - m1;
+    double *A = X, *B = X + ld * m1, *C = X + m1 + ld * m1;
+    double *W = scratch, *V = scratch + m1 * m2, *inner = scratch + 2 * m1 * m2;
+    if ((st = spd_inverse_seed(A, ld, m1, inner, w, s))) return st;                                    // X_A
+    if ((st = seed_product(w, A, 1, ld, B, ld, 1, m1, m2, m1, false, 1.0, 0.0, W, m1, s))) return st;   // W = X_A B
+    if ((st = seed_product(w, B, ld, 1, W, m1, 1, m2, m2, m1, true, -1.0, 1.0, C, ld, s))) return st;   // S = C - B^T W
+    if ((st = spd_inverse_seed(C, ld, m2, inner, w, s))) return st;                                    // X_S
+    if ((st = seed_product(w, W, 1, m1, C, ld, 1, m1, m2, m2, false, 1.0, 0.0, V, m1, s))) return st;   // V = W X_S
+    if ((st = seed_product(w, V, 1, m1, W, 1, m1, m1, m1, m2, true, 1.0, 1.0, A, ld, s))) return st;    // X_A += V W^T
+    seed_offdiag_kernel<<<seed_grid(m1 * m2), 256, 0, s>>>(V, m1, m2, X, ld);
+    count_launch();
+    SMX_TRY_CUDA(cudaGetLastError());
+    return SMX_OK;
+}
+
 }  // namespace smx
 
 using namespace smx;
@@ -246,5 +382,74 @@ extern "C" int smx_spd_inverse_f32(const double *G, int64_t m, float *Xinv, void
     SMX_TRY_CUDA(cudaMemcpyAsync(&hflag, flag, sizeof(int), cudaMemcpyDeviceToHost, s));
     SMX_TRY_CUDA(cudaStreamSynchronize(s));
     if (hflag) return set_error(SMX_ERR_NUMERIC, "smx_spd_inverse_f32: a pivot was not positive");
+    return SMX_OK;
+}
+
+namespace {
+struct SeedLayout {
+    split::Operand a, b;
+    size_t a_sl, a_e, b_sl, b_e, T, R, rowmax, scratch, gp, gjws, err, total;
+};
+SeedLayout seed_layout(int64_t m) {
+    SeedLayout L;
+    L.a = split::make_operand(m, m, split::MT, 4);
+    L.b = split::make_operand(m, m, split::MT, 4);
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off = (off + bytes + 255) & ~(size_t)255; return o; };
+    const int64_t mb = m < kSeedBaseRows ? m : kSeedBaseRows, mp = spd_inverse_padded(mb);
+    L.a_sl = take(L.a.slice_bytes());
+    L.a_e = take(L.a.row_tiles * split::MT * sizeof(int32_t));
+    L.b_sl = take(L.b.slice_bytes());
+    L.b_e = take(L.b.row_tiles * split::MT * sizeof(int32_t));
+    L.T = take((size_t)m * m * sizeof(unsigned long long));
+    L.R = take((size_t)m * m * sizeof(float));
+    L.rowmax = take((size_t)m * sizeof(unsigned long long));
+    L.scratch = take((size_t)m * m * sizeof(double));
+    L.gp = take((size_t)mp * mp * sizeof(float));
+    L.gjws = take(spd_inverse_workspace(mb));
+    L.err = take(4 * sizeof(int));
+    L.total = off;
+    return L;
+}
+}  // namespace
+
+extern "C" int smx_spd_inverse_seed_workspace_size(int64_t m, size_t *bytes) {
+    if (m < 1 || m > 46340 || !bytes) return set_error(SMX_ERR_ARGUMENT, "smx_spd_inverse_seed_workspace_size: bad argument");
+    *bytes = seed_layout(m).total;
+    return SMX_OK;
+}
+
+extern "C" int smx_spd_inverse_seed(const double *G, int64_t m, double *X, void *workspace, size_t workspace_bytes,
+                                    void *stream) {
+    if (m < 1 || m > 46340 || !G || !X || !workspace)
+        return set_error(SMX_ERR_ARGUMENT, "smx_spd_inverse_seed: bad argument");
+    const SeedLayout L = seed_layout(m);
+    if (workspace_bytes < L.total)
+        return set_error(SMX_ERR_WORKSPACE, "smx_spd_inverse_seed: workspace %zu < %zu bytes", workspace_bytes, L.total);
+    cudaStream_t s = (cudaStream_t)stream;
+    unsigned char *ws = (unsigned char *)workspace;
+    SeedWorkspace w;
+    w.a_slices = (__nv_bfloat16 *)(ws + L.a_sl);
+    w.a_expo = (int32_t *)(ws + L.a_e);
+    w.b_slices = (__nv_bfloat16 *)(ws + L.b_sl);
+    w.b_expo = (int32_t *)(ws + L.b_e);
+    w.T = (unsigned long long *)(ws + L.T);
+    w.R = (float *)(ws + L.R);
+    w.rowmax = (unsigned long long *)(ws + L.rowmax);
+    w.gp = (float *)(ws + L.gp);
+    w.gjws = (float *)(ws + L.gjws);
+    w.err = (int *)(ws + L.err);
+    w.flag = w.err + 1;
+    SMX_TRY_CUDA(cudaMemsetAsync(w.T, 0, (size_t)m * m * sizeof(unsigned long long), s));
+    SMX_TRY_CUDA(cudaMemsetAsync(w.R, 0, (size_t)m * m * sizeof(float), s));
+    SMX_TRY_CUDA(cudaMemsetAsync(w.err, 0, 4 * sizeof(int), s));
+    SMX_TRY_CUDA(cudaMemcpyAsync(X, G, (size_t)m * m * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    int st = spd_inverse_seed(X, m, m, (double *)(ws + L.scratch), w, s);
+    if (st) return st;
+    int herr[2] = {0, 0};
+    SMX_TRY_CUDA(cudaMemcpyAsync(herr, w.err, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    SMX_TRY_CUDA(cudaStreamSynchronize(s));
+    if (herr[0]) return set_error(SMX_ERR_CUDA, "smx_spd_inverse_seed: product kernel gave up waiting (code %d)", herr[0]);
+    if (herr[1]) return set_error(SMX_ERR_NUMERIC, "smx_spd_inverse_seed: a pivot was not positive");
     return SMX_OK;
 }

@@ -1,10 +1,13 @@
 // FP64-accurate products on the bf16 tensor cores: the sliced GEMM kernel and
 // the slicing kernels (method and number format in split_gemm.cuh).
 //
-// Kernel layout (one CTA per SM, stream-K over (output tile, k tile) units):
-//   warp 0      producer: one cp.async.bulk per slice tile into a STAGES-deep ring
-//               (the slices are stored in global memory in the shared-memory tile
-//               layout, so a tile is one contiguous copy; no tensor map);
+// Kernel layout (one CTA per SM, stream-K over (output tile, k step) units; a k step
+// is half a k tile, KS = 16, one MMA per slice pair):
+//   warp 0      producer: one cp.async.bulk per slice and k step into a ring of as
+//               many stages as fit in shared memory (the slices are stored in global
+//               memory in the shared-memory tile layout, K-major core matrices, so a
+//               half tile is one contiguous copy; no tensor map).  Only the slices
+//               that take part in some pair s + t <= LMAX are loaded;
 //   warp 1      owns the tensor memory and issues tcgen05.mma from one thread;
 //   warps 2..9  epilogue: at the end of every exact chunk they read the level 2/3
 //               accumulators (tcgen05.ld) into int32 running sums; at the end of
@@ -121,6 +124,7 @@ struct GemmParams {
     const __nv_bfloat16 *A, *B;
     int64_t a_slice, b_slice;            // elements between slices
     int64_t a_row_tiles, b_row_tiles, k_tiles;
+    int64_t k_steps;                     // KS-wide k steps per output tile (2 k_tiles)
     int64_t M, N;                        // logical output size
     int64_t n_tiles_out;                 // output tiles along N
     int64_t units;                       // total (tile, k tile) units
@@ -146,11 +150,17 @@ __device__ __forceinline__ void tile_coords(const GemmParams &p, int64_t tile, i
     }
 }
 
-template <int SA, int SB, int LMAX, int NT, int EXACT, int STAGES>
+// k per pipeline stage: KSUB MMAs of K = 16 (the first or second half of a KT tile for
+// KSUB = 1, a whole tile for KSUB = 2)
+template <int SA, int SB, int LMAX, int NT, int EXACT, int STAGES, int KSUB>
 struct Cfg {
-    static constexpr uint32_t A_TILE = MT * KT * 2;        // bytes of one slice tile
-    static constexpr uint32_t B_TILE = NT * KT * 2;
-    static constexpr uint32_t STAGE = SA * A_TILE + SB * B_TILE;
+    static constexpr int KS = 16 * KSUB;
+    // slices that take part in some pair s + t <= LMAX (the others are never loaded)
+    static constexpr int UA = SA < LMAX - 1 ? SA : LMAX - 1;
+    static constexpr int UB = SB < LMAX - 1 ? SB : LMAX - 1;
+    static constexpr uint32_t A_STEP = MT * KS * 2;        // bytes of one slice's k step
+    static constexpr uint32_t B_STEP = NT * KS * 2;
+    static constexpr uint32_t STAGE = UA * A_STEP + UB * B_STEP;
     static constexpr uint32_t SMEM = STAGES * STAGE + 256;
     static constexpr int HALF = NT / 2;                     // columns per epilogue warp
     static constexpr int THREADS = 320;
@@ -158,13 +168,23 @@ struct Cfg {
     static constexpr int ACC_STRIDE = (NT + 31) / 32 * 32;
     // the exact levels' sums stay below 2^24 units over 1024 / (pairs per level) k
     static constexpr int MAXP = EXACT < (SA < SB ? SA : SB) ? EXACT : (SA < SB ? SA : SB);
-    static constexpr int CHUNK_KT = (MAXP < 1 ? 1024 : 1024 / MAXP) / KT;
-    static_assert(CHUNK_KT >= 1, "chunk");
+    static constexpr int CHUNK_KS = (MAXP < 1 ? 1024 : 1024 / MAXP) / KS;
+    static constexpr int OUT_KS = OUT_KT * KT / KS;
+    static_assert(CHUNK_KS >= 1, "chunk");
+    static_assert(KT % KS == 0, "stage k");
 };
 
-template <int SA, int SB, int LMAX, int NT, int EXACT, int STAGES>
+// ring depth: as many stages as fit in 227 KB next to the barriers, at most 8
+template <int SA, int SB, int LMAX, int NT, int EXACT, int KSUB>
+constexpr int stages_for() {
+    constexpr uint32_t st = Cfg<SA, SB, LMAX, NT, EXACT, 1, KSUB>::STAGE;
+    constexpr int n = (int)((232448u - 256u) / st);
+    return n > 8 ? 8 : n;
+}
+
+template <int SA, int SB, int LMAX, int NT, int EXACT, int STAGES, int KSUB>
 __global__ void __launch_bounds__(320, 1) gemm_kernel(const GemmParams p) {
-    using C = Cfg<SA, SB, LMAX, NT, EXACT, STAGES>;
+    using C = Cfg<SA, SB, LMAX, NT, EXACT, STAGES, KSUB>;
     static_assert(NT % 16 == 0 && NT <= 128 && NT >= 16, "N tile");
     static_assert(C::HALF % 8 == 0, "epilogue columns in groups of 8");
     static_assert((EXACT + 1) * C::ACC_STRIDE <= 512, "tensor memory");
@@ -204,31 +224,46 @@ __global__ void __launch_bounds__(320, 1) gemm_kernel(const GemmParams p) {
     dev::fence_after();
     const uint32_t tmem = *tmem_holder;
 
-    // flush schedule shared by the MMA issuer and the epilogue: after unit u,
-    // flush if the chunk is full, the output flush distance is reached or the tile ends
+    // The three roles walk the same units u0 .. u1 - 1 with running counters (k step
+    // within the tile, ring stage and its phase) instead of 64-bit divisions per unit.
+    // Flush schedule shared by the MMA issuer and the epilogue: after unit u, flush if
+    // the chunk is full, the output flush distance is reached or the tile ends.
     if (warp == 0) {
         if (lane == 0) {
+            int stage = 0;
+            uint32_t par = 0;                        // parity of the ring round
             int64_t it = 0;
+            int64_t tile = u0 / p.k_steps, ks = u0 % p.k_steps;
+            int64_t mt, nt;
+            tile_coords(p, tile, mt, nt);
             for (int64_t u = u0; u < u1; ++u, ++it) {
-                const int stage = (int)(it % STAGES);
-                if (it >= STAGES && !dev::mbar_wait(empty + stage, (uint32_t)((it / STAGES - 1) & 1), abort_flag)) {
+                // a stage is refilled once the MMAs of its previous round have completed
+                if (it >= STAGES && !dev::mbar_wait(empty + stage, par ^ 1u, abort_flag)) {
                     atomicExch(p.err, 1);
                     *abort_flag = 1;
                     break;
                 }
-                const int64_t tile = u / p.k_tiles, kt = u % p.k_tiles;
-                int64_t mt, nt;
-                tile_coords(p, tile, mt, nt);
+                // tiles are contiguous along k, so k step ks of row tile mt starts at
+                // (mt k_steps + ks) MT KS elements of a slice
                 unsigned char *sbase = smem + stage * C::STAGE;
+                const __nv_bfloat16 *ga = p.A + (mt * p.k_steps + ks) * (MT * C::KS);
+                const __nv_bfloat16 *gb = p.B + (nt * p.k_steps + ks) * (NT * C::KS);
                 dev::mbar_expect_tx(full + stage, C::STAGE);
 #pragma unroll
-                for (int s = 0; s < SA; ++s)
-                    dev::bulk_g2s(sbase + s * C::A_TILE, p.A + s * p.a_slice + (mt * p.k_tiles + kt) * (MT * KT),
-                                  C::A_TILE, full + stage);
+                for (int s = 0; s < C::UA; ++s)
+                    dev::bulk_g2s(sbase + s * C::A_STEP, ga + s * p.a_slice, C::A_STEP, full + stage);
 #pragma unroll
-                for (int t = 0; t < SB; ++t)
-                    dev::bulk_g2s(sbase + SA * C::A_TILE + t * C::B_TILE,
-                                  p.B + t * p.b_slice + (nt * p.k_tiles + kt) * (NT * KT), C::B_TILE, full + stage);
+                for (int t = 0; t < C::UB; ++t)
+                    dev::bulk_g2s(sbase + C::UA * C::A_STEP + t * C::B_STEP, gb + t * p.b_slice, C::B_STEP,
+                                  full + stage);
+                if (++stage == STAGES) {
+                    stage = 0;
+                    par ^= 1u;
+                }
+                if (++ks == p.k_steps) {
+                    ks = 0;
+                    tile_coords(p, ++tile, mt, nt);
+                }
             }
             // no bulk copy may still be landing in shared memory when the CTA leaves:
             // wait for the last STAGES issued stages (each has exactly one phase
@@ -241,22 +276,29 @@ __global__ void __launch_bounds__(320, 1) gemm_kernel(const GemmParams p) {
         if (lane == 0) {
             constexpr uint32_t ID = dev::idesc(MT, NT);
             constexpr uint32_t LBO_A = (MT / 8) * 128, LBO_B = (NT / 8) * 128, SBO = 128;
-            int64_t it = 0;
+            // descriptors of stage 0's first slices; a stage or slice offset is added to
+            // the address field (shared addresses stay below 2^18, so it cannot carry)
+            const uint32_t s0 = dev::smem_u32(smem);
+            const uint64_t a_desc0 = dev::desc(s0, LBO_A, SBO);
+            const uint64_t b_desc0 = dev::desc(s0 + C::UA * C::A_STEP, LBO_B, SBO);
+            int stage = 0;
+            uint32_t par = 0;
+            int64_t ks = u0 % p.k_steps;
             int since_chunk = 0, since_out = 0;
             uint32_t flushes = 0;
             uint32_t fresh = (1u << (EXACT + 1)) - 1;   // accumulators to overwrite on their next MMA
             bool pending = false;                       // a chunk flush whose read-out has not been confirmed
             // one unit's MMAs of the exact levels (EXACTS = true) or of the rounded one
-            auto issue = [&](uint32_t sa, uint32_t sb, bool exacts) {
+            auto issue = [&](uint64_t ad0, uint64_t bd0, bool exacts) {
 #pragma unroll
-                for (int j = 0; j < KT / 16; ++j) {
+                for (int j = 0; j < KSUB; ++j) {
 #pragma unroll
-                    for (int s = 1; s <= SA; ++s) {
+                    for (int s = 1; s <= C::UA; ++s) {
 #pragma unroll
-                        for (int t = 1; t <= SB; ++t) {
+                        for (int t = 1; t <= C::UB; ++t) {
                             if (s + t <= LMAX && ((s + t - 2 < EXACT) == exacts)) {
-                                const uint64_t ad = dev::desc(sa + (s - 1) * C::A_TILE + j * 2 * LBO_A, LBO_A, SBO);
-                                const uint64_t bd = dev::desc(sb + (t - 1) * C::B_TILE + j * 2 * LBO_B, LBO_B, SBO);
+                                const uint64_t ad = ad0 + (((s - 1) * C::A_STEP + j * 2 * LBO_A) >> 4);
+                                const uint64_t bd = bd0 + (((t - 1) * C::B_STEP + j * 2 * LBO_B) >> 4);
                                 const int acc = (s + t - 2) < EXACT ? (s + t - 2) : EXACT;
                                 dev::mma(tmem + acc * C::ACC_STRIDE, ad, bd, ID, (fresh >> acc) & 1u ? 0u : 1u);
                                 fresh &= ~(1u << acc);
@@ -265,19 +307,18 @@ __global__ void __launch_bounds__(320, 1) gemm_kernel(const GemmParams p) {
                     }
                 }
             };
-            for (int64_t u = u0; u < u1; ++u, ++it) {
-                const int stage = (int)(it % STAGES);
-                if (!dev::mbar_wait(full + stage, (uint32_t)((it / STAGES) & 1), abort_flag)) {
+            for (int64_t u = u0; u < u1; ++u) {
+                if (!dev::mbar_wait(full + stage, par, abort_flag)) {
                     atomicExch(p.err, 2);
                     *abort_flag = 1;
                     break;
                 }
                 dev::fence_after();
-                const uint32_t sa = dev::smem_u32(smem + stage * C::STAGE);
-                const uint32_t sb = sa + SA * C::A_TILE;
+                const uint64_t soff = (uint64_t)((stage * C::STAGE) >> 4);
+                const uint64_t ad0 = a_desc0 + soff, bd0 = b_desc0 + soff;
                 // the rounded level is not read at a chunk flush, so its MMAs go first
                 // while the epilogue still reads the exact levels of the previous chunk
-                issue(sa, sb, false);
+                issue(ad0, bd0, false);
                 if (pending) {
                     if (!dev::mbar_wait(acc_empty, (flushes - 1) & 1, abort_flag)) {
                         atomicExch(p.err, 3);
@@ -287,13 +328,18 @@ __global__ void __launch_bounds__(320, 1) gemm_kernel(const GemmParams p) {
                     dev::fence_after();
                     pending = false;
                 }
-                issue(sa, sb, true);
+                issue(ad0, bd0, true);
                 dev::commit(empty + stage);
+                if (++stage == STAGES) {
+                    stage = 0;
+                    par ^= 1u;
+                }
                 ++since_chunk;
                 ++since_out;
-                const bool tile_end = (u % p.k_tiles == p.k_tiles - 1) || (u + 1 == u1);
-                const bool out_flush = tile_end || since_out == OUT_KT;
-                if (out_flush || since_chunk == C::CHUNK_KT) {
+                const bool tile_end = (ks == p.k_steps - 1) || (u + 1 == u1);
+                if (++ks == p.k_steps) ks = 0;
+                const bool out_flush = tile_end || since_out == C::OUT_KS;
+                if (out_flush || since_chunk == C::CHUNK_KS) {
                     dev::commit(acc_full);
                     ++flushes;
                     fresh |= (1u << EXACT) - 1;
@@ -332,12 +378,14 @@ __global__ void __launch_bounds__(320, 1) gemm_kernel(const GemmParams p) {
         for (int c = 0; c < C::HALF; ++c) sum[c] = 0;
         int since_chunk = 0, since_out = 0;
         uint32_t flushes = 0;
+        int64_t ks = u0 % p.k_steps;
         for (int64_t u = u0; u < u1; ++u) {
             ++since_chunk;
             ++since_out;
-            const bool tile_end = (u % p.k_tiles == p.k_tiles - 1) || (u + 1 == u1);
-            const bool out_flush = tile_end || since_out == OUT_KT;
-            if (!(out_flush || since_chunk == C::CHUNK_KT)) continue;
+            const bool tile_end = (ks == p.k_steps - 1) || (u + 1 == u1);
+            if (++ks == p.k_steps) ks = 0;
+            const bool out_flush = tile_end || since_out == C::OUT_KS;
+            if (!(out_flush || since_chunk == C::CHUNK_KS)) continue;
             // every lane waits, and the warp goes on only if all of them saw the phase
             // complete, so that the .sync.aligned tensor-memory loads below run with the
             // full warp or not at all
@@ -352,7 +400,7 @@ __global__ void __launch_bounds__(320, 1) gemm_kernel(const GemmParams p) {
             ++flushes;
             dev::fence_after();
             int64_t mt = 0, nt = 0;
-            if (out_flush) tile_coords(p, u / p.k_tiles, mt, nt);
+            if (out_flush) tile_coords(p, u / p.k_steps, mt, nt);
             const int64_t gi = mt * MT + row;
 #pragma unroll
             for (int c0 = 0; c0 < C::HALF; c0 += 8) {
@@ -485,14 +533,19 @@ __global__ void slice_rows_kernel(const T *__restrict__ src, int64_t sr, int64_t
 
 // ------------------------------------------------------------------ host side
 
+// Stages of a whole KT tile (two MMAs of K = 16 per slice pair).  Half-tile stages fit
+// twice as many stages in shared memory, but ran the config-1 NNLS 10 % slower
+// (200 ms against 182 ms per solve on one GB300).
+constexpr int kStageSub = 2;
+
 template <int SA, int SB, int LMAX, int NT, int EXACT>
 static int launch_gemm(const Operand &A, const Operand &B, const Acc &acc, bool lower_only, int *err, cudaStream_t s,
                        const int *skip) {
-    // as many stages as fit in 227 KB of shared memory (2 or 3)
-    constexpr int STAGES = Cfg<SA, SB, LMAX, NT, EXACT, 3>::SMEM <= 232448 ? 3 : 2;
-    using C = Cfg<SA, SB, LMAX, NT, EXACT, STAGES>;
-    static_assert(C::SMEM <= 232448, "shared memory");
-    SMX_TRY_CUDA(cudaFuncSetAttribute(gemm_kernel<SA, SB, LMAX, NT, EXACT, STAGES>,
+    constexpr int KSUB = kStageSub;
+    constexpr int STAGES = stages_for<SA, SB, LMAX, NT, EXACT, KSUB>();
+    using C = Cfg<SA, SB, LMAX, NT, EXACT, STAGES, KSUB>;
+    static_assert(STAGES >= 2 && C::SMEM <= 232448, "shared memory");
+    SMX_TRY_CUDA(cudaFuncSetAttribute(gemm_kernel<SA, SB, LMAX, NT, EXACT, STAGES, KSUB>,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM));
     int dev = 0, sms = 0;
     SMX_TRY_CUDA(cudaGetDevice(&dev));
@@ -505,12 +558,13 @@ static int launch_gemm(const Operand &A, const Operand &B, const Acc &acc, bool 
     p.a_row_tiles = A.row_tiles;
     p.b_row_tiles = B.row_tiles;
     p.k_tiles = A.k_tiles;
+    p.k_steps = A.k_tiles * (KT / C::KS);
     p.M = A.rows;
     p.N = B.rows;
     p.n_tiles_out = B.row_tiles;
     p.lower_only = lower_only ? 1 : 0;
     const int64_t tiles = lower_only ? A.row_tiles * (A.row_tiles + 1) / 2 : A.row_tiles * B.row_tiles;
-    p.units = tiles * A.k_tiles;
+    p.units = tiles * p.k_steps;
     p.T = acc.T;
     p.R = acc.R;
     p.ld = acc.ld;
@@ -518,7 +572,7 @@ static int launch_gemm(const Operand &A, const Operand &B, const Acc &acc, bool 
     p.skip = skip;
     int64_t grid = sms;
     if (grid > p.units) grid = p.units;
-    gemm_kernel<SA, SB, LMAX, NT, EXACT, STAGES><<<(unsigned)grid, C::THREADS, C::SMEM, s>>>(p);
+    gemm_kernel<SA, SB, LMAX, NT, EXACT, STAGES, KSUB><<<(unsigned)grid, C::THREADS, C::SMEM, s>>>(p);
     count_launch();
     SMX_TRY_CUDA(cudaGetLastError());
     return SMX_OK;
@@ -552,6 +606,10 @@ int gemm(const Operand &A, const Operand &B, const Acc &acc, bool lower_only, in
         return launch_gemm<4, 5, 5, 112, 3>(A, B, acc, lower_only, err, s, skip);
     if (B.tile_rows == 128 && key == 54 && lmax == 6)
         return launch_gemm<5, 4, 6, 128, 3>(A, B, acc, lower_only, err, s, skip);
+    if (B.tile_rows == 128 && key == 44 && lmax == 5)
+        return launch_gemm<4, 4, 5, 128, 3>(A, B, acc, lower_only, err, s, skip);
+    if (B.tile_rows == 96 && key == 77 && lmax == 7)
+        return launch_gemm<7, 7, 7, 96, 4>(A, B, acc, lower_only, err, s, skip);
     if (lmax != 0) return set_error(SMX_ERR_UNSUPPORTED, "split gemm: no kernel with pairs up to s + t = %d", lmax);
     if (B.tile_rows == 112) {
         switch (key) {

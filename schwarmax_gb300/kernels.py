@@ -273,6 +273,19 @@ def spd_inverse_f32(G):
     return X
 
 
+def spd_inverse_seed(G):
+    """Seed inverse of a symmetric positive definite double CUDA matrix by Schur-complement
+    recursion on split products (smx_spd_inverse_seed); double, exactly symmetric."""
+    m = G.shape[0]
+    _check(G, "G", torch.float64, (m, m))
+    nbytes = ctypes.c_size_t(0)
+    call("smx_spd_inverse_seed_workspace_size", m, ctypes.byref(nbytes))
+    ws = torch.empty(nbytes.value, dtype=torch.uint8, device=G.device)
+    X = torch.empty(m, m, dtype=torch.float64, device=G.device)
+    call("smx_spd_inverse_seed", _ptr(G), m, _ptr(X), _ptr(ws), ws.numel(), _stream())
+    return X
+
+
 def split_gemm(A, B, a_slices=4, b_slices=4, lower=False):
     """C = A @ B for double CUDA tensors A (M, K), B (K, N) through the split
     (Ozaki) tensor-core product smx_split_gemm; returns C (M, N) double.
