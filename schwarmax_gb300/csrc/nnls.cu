@@ -116,7 +116,7 @@ struct Layout {
     // split path
     size_t Tacc, Racc, rowmax, err;
     size_t Ua, Ua_e, Ut, Ut_e, Xg, Xg_e, Ds, Ds_e, Es, Es_e, Fs, Fs_e;
-    size_t G7, G7_e, X7, X7_e, X4, X4_e, R4, R4_e, Gf, gjws, nsflag, Xd, Rd, Ebuf, Fbuf, gdiag, colmax;
+    size_t G7, G7_e, X7, X7_e, X4, X4_e, R4, R4_e, Gf, gjws, seedbase, nsflag, Xd, Rd, Ebuf, Fbuf, gdiag, colmax;
     int lwork_s;   // float Cholesky / inverse scratch (floats)
     int64_t acc_elems;
     size_t work_bytes, host_bytes;   // device / host scratch of the factorisation and inversion
@@ -182,6 +182,7 @@ static int layout(const smx_nnls_problem *p, Layout *L, cusolverDnHandle_t solve
         const int64_t mp = spd_inverse_padded(mb);
         L->Gf = take((size_t)mp * mp * sizeof(float));
         L->gjws = take(spd_inverse_workspace(mb));
+        L->seedbase = take((size_t)2 * mb * mb * sizeof(double));
         L->nsflag = take(16 * sizeof(int));
         L->Xd = take(m * m * sizeof(double));
         L->Rd = take(m * m * sizeof(double));
@@ -690,6 +691,7 @@ static int mixed_setup(const smx_nnls_problem *p, const TL *lib, const int32_t *
         sw.rowmax = rowmax;
         sw.gp = Gp;
         sw.gjws = (float *)(ws + L.gjws);
+        sw.base = (double *)(ws + L.seedbase);
         sw.err = derr;
         sw.flag = dinfo + 1;
         SMX_TRY_CUDA(cudaMemcpyAsync(Xd, G, (size_t)m * m * sizeof(double), cudaMemcpyDeviceToDevice, s));

@@ -218,17 +218,17 @@ int spd_inverse_inplace(float *Ap, int64_t mp, float *ws, int *flag, cudaStream_
 //   G = [A B; B^T C]:  X_A = A^-1,  W = X_A B,  S = C - B^T W,  X_S = S^-1,
 //   V = W X_S,  G^-1 = [X_A + V W^T, -V; -V^T, X_S],
 // with A^-1 and S^-1 by the same rule down to blocks of at most kSeedBaseRows rows, which
-// the FP32 Gauss-Jordan above inverts.  The four products of a level run on the split
-// tensor-core kernel with 4 slices and pairs s + t <= 5 (31 bits of every row's and
-// column's largest magnitude), so the result has the quality of an FP32 inverse; the
+// the FP32 Gauss-Jordan above inverts and one Newton-Schulz step (R = I - A X,
+// X += X R) refines.  Every product runs on the split tensor-core kernel with 5 slices
+// and pairs s + t <= 6 (39 bits of every row's and column's largest magnitude); the
 // products are about m^3 flops per slice pair in all.  The Schur complements of an SPD
 // matrix are SPD, so no pivoting is needed.  The result is exactly symmetric (the
 // symmetric products are formed on their lower tiles and mirrored).
 
 namespace {
 
-constexpr int kSeedSlices = 4;
-constexpr int kSeedLevels = 5;        // slice pairs s + t <= 5
+constexpr int kSeedSlices = 5;
+constexpr int kSeedLevels = 6;        // slice pairs s + t <= 6
 
 __device__ __forceinline__ double exp2i(int p) { return __longlong_as_double((long long)(1023 + p) << 52); }
 
@@ -279,6 +279,15 @@ __global__ void seed_pad_kernel(const double *__restrict__ X, int64_t ld, int64_
     }
 }
 
+// B (m x m, leading dimension m) = the block at X (leading dimension ld); I = identity in R
+__global__ void seed_copy_kernel(const double *__restrict__ X, int64_t ld, int64_t m, double *B, double *R) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < m * m; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = e % m, c = e / m;
+        B[e] = X[r + ld * c];
+        R[e] = r == c ? 1.0 : 0.0;
+    }
+}
+
 // the block back in double, symmetrised
 __global__ void seed_unpad_kernel(const float *__restrict__ Ap, int64_t mp, double *X, int64_t ld, int64_t m) {
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < m * m; e += (int64_t)gridDim.x * blockDim.x) {
@@ -325,11 +334,15 @@ int spd_inverse_seed(double *X, int64_t ld, int64_t m, double *scratch, const Se
     int st;
     if (m <= kSeedBaseRows) {
         const int64_t mp = spd_inverse_padded(m);
+        double *A0 = w.base, *R = w.base + m * m;
+        seed_copy_kernel<<<seed_grid(m * m), 256, 0, s>>>(X, ld, m, A0, R);
         seed_pad_kernel<<<seed_grid(mp * mp), 256, 0, s>>>(X, ld, m, w.gp, mp);
-        count_launch();
+        count_launch(2);
         if ((st = spd_inverse_inplace(w.gp, mp, w.gjws, w.flag, s))) return st;
         seed_unpad_kernel<<<seed_grid(m * m), 256, 0, s>>>(w.gp, mp, X, ld, m);
         count_launch();
+        if ((st = seed_product(w, A0, 1, m, X, ld, 1, m, m, m, false, -1.0, 1.0, R, m, s))) return st;   // R = I - A X
+        if ((st = seed_product(w, X, 1, ld, R, m, 1, m, m, m, true, 1.0, 1.0, X, ld, s))) return st;     // X += X R
         SMX_TRY_CUDA(cudaGetLastError());
         return SMX_OK;
     }
@@ -388,12 +401,12 @@ extern "C" int smx_spd_inverse_f32(const double *G, int64_t m, float *Xinv, void
 namespace {
 struct SeedLayout {
     split::Operand a, b;
-    size_t a_sl, a_e, b_sl, b_e, T, R, rowmax, scratch, gp, gjws, err, total;
+    size_t a_sl, a_e, b_sl, b_e, T, R, rowmax, scratch, base, gp, gjws, err, total;
 };
 SeedLayout seed_layout(int64_t m) {
     SeedLayout L;
-    L.a = split::make_operand(m, m, split::MT, 4);
-    L.b = split::make_operand(m, m, split::MT, 4);
+    L.a = split::make_operand(m, m, split::MT, kSeedSlices);
+    L.b = split::make_operand(m, m, split::MT, kSeedSlices);
     size_t off = 0;
     auto take = [&](size_t bytes) { size_t o = off; off = (off + bytes + 255) & ~(size_t)255; return o; };
     const int64_t mb = m < kSeedBaseRows ? m : kSeedBaseRows, mp = spd_inverse_padded(mb);
@@ -405,6 +418,7 @@ SeedLayout seed_layout(int64_t m) {
     L.R = take((size_t)m * m * sizeof(float));
     L.rowmax = take((size_t)m * sizeof(unsigned long long));
     L.scratch = take((size_t)m * m * sizeof(double));
+    L.base = take((size_t)2 * mb * mb * sizeof(double));
     L.gp = take((size_t)mp * mp * sizeof(float));
     L.gjws = take(spd_inverse_workspace(mb));
     L.err = take(4 * sizeof(int));
@@ -438,6 +452,7 @@ extern "C" int smx_spd_inverse_seed(const double *G, int64_t m, double *X, void 
     w.rowmax = (unsigned long long *)(ws + L.rowmax);
     w.gp = (float *)(ws + L.gp);
     w.gjws = (float *)(ws + L.gjws);
+    w.base = (double *)(ws + L.base);
     w.err = (int *)(ws + L.err);
     w.flag = w.err + 1;
     SMX_TRY_CUDA(cudaMemsetAsync(w.T, 0, (size_t)m * m * sizeof(unsigned long long), s));

@@ -608,6 +608,8 @@ int gemm(const Operand &A, const Operand &B, const Acc &acc, bool lower_only, in
         return launch_gemm<5, 4, 6, 128, 3>(A, B, acc, lower_only, err, s, skip);
     if (B.tile_rows == 128 && key == 44 && lmax == 5)
         return launch_gemm<4, 4, 5, 128, 3>(A, B, acc, lower_only, err, s, skip);
+    if (B.tile_rows == 128 && key == 55 && lmax == 6)
+        return launch_gemm<5, 5, 6, 128, 3>(A, B, acc, lower_only, err, s, skip);
     if (B.tile_rows == 96 && key == 77 && lmax == 7)
         return launch_gemm<7, 7, 7, 96, 4>(A, B, acc, lower_only, err, s, skip);
     if (lmax != 0) return set_error(SMX_ERR_UNSUPPORTED, "split gemm: no kernel with pairs up to s + t = %d", lmax);

@@ -138,7 +138,8 @@ int exact_levels(const Operand &A, const Operand &B);
 // requires A.tile_rows == B.tile_rows).  err receives a nonzero code if a wait
 // in the kernel gave up.
 // lmax = 0 forms every slice pair; lmax = 5, 6 or 7 (4 x 5 slices, 112-wide tiles), 6
-// (5 x 4 slices, 128-wide tiles), 5 (4 x 4 slices, 128-wide tiles) or 7 (7 x 7 slices,
+// (5 x 4 slices, 128-wide tiles), 5 (4 x 4 slices, 128-wide tiles), 6 (5 x 5 slices,
+// 128-wide tiles) or 7 (7 x 7 slices,
 // 96-wide tiles) drops the pairs s + t > lmax, about 2^-8(lmax-1) of max|A| max|B| per
 // product term; slices that take part in no remaining pair are not read.
 // skip (optional device flag): when *skip != 0 at run time the launched kernels
@@ -157,11 +158,12 @@ int slice_rows(const T *src, int64_t sr, int64_t sc, const Operand &op, unsigned
 }  // namespace split
 
 // Seed of G^-1 for a symmetric positive definite G (spd_inverse.cu): recursive Schur
-// complements on the split products above, FP32 Gauss-Jordan on blocks of up to
-// kSeedBaseRows rows.  Buffers (device): a/b slices and exponents for operands of up to m x m (4
-// slices, 128-row tiles), T/R accumulators of m x m (zero on entry, left zero), rowmax
-// (m), the padded float block and Gauss-Jordan scratch for kSeedBaseRows rows, err (product
-// waits that gave up) and flag (set when a pivot was not positive).
+// complements on the split products above, FP32 Gauss-Jordan and one Newton-Schulz step
+// on blocks of up to kSeedBaseRows rows.  Buffers (device): a/b slices and exponents for
+// operands of up to m x m (5 slices, 128-row tiles), T/R accumulators of m x m (zero on
+// entry, left zero), rowmax (m), the padded float block and Gauss-Jordan scratch for
+// kSeedBaseRows rows, base (2 kSeedBaseRows^2 doubles: a block's input and residual),
+// err (product waits that gave up) and flag (set when a pivot was not positive).
 constexpr int64_t kSeedBaseRows = 1024;
 struct SeedWorkspace {
     __nv_bfloat16 *a_slices, *b_slices;
@@ -170,6 +172,7 @@ struct SeedWorkspace {
     float *R;
     unsigned long long *rowmax;
     float *gp, *gjws;
+    double *base;
     int *err, *flag;
 };
 int spd_inverse_seed(double *X, int64_t ld, int64_t m, double *scratch, const SeedWorkspace &w, cudaStream_t s);
