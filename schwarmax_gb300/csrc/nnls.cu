@@ -23,9 +23,9 @@
 // FP64-grade accuracy by Ozaki splitting (split_gemm.cuh): U in 4 slices (31 bits
 // below each row's or column's largest magnitude), the iterates' vectors in 5
 // (39 bits), G^-1 in 5, H = G^-1 U in 4.  G = U U^T + cI is formed from the slices
-// of U; G^-1 starts from a float Gauss-Jordan inverse and is refined by
-// Newton-Schulz steps whose residual products use 7 slices; the iterates z, u, D
-// stay in double.
+// of U; G^-1 starts from a seed by Schur-complement recursion on split products
+// (spd_inverse.cu, residual ~4e-5) and is refined by a Newton-Schulz step whose
+// residual product uses 7 slices; the iterates z, u, D stay in double.
 // At 16384 orbits (cond(G) = 1.8e3) the weights move the chi^2 by about 0.02
 // when U is rounded to float, by about 40 when G^-1 is stored in float and by
 // about 500 when the iterations run in float arithmetic, which is why the
@@ -300,7 +300,10 @@ enum { COL_INIT = 0, COL_RESID = 1, COL_PLAIN = 2, COL_UPDATE = 3 };
 
 constexpr int kNsMaxSteps = 5;   // Newton-Schulz steps at most (a seed residual of 0.2 needs 4)
 constexpr double kNsStopResidual2 = 1e-8;   // ||R||_F^2 of the input of the last step
-constexpr int kNsResidualLevels = 7;   // slice pairs s + t <= 7 of the residual G X (7 x 7 slices)
+// Slice pairs s + t <= 7 of the residual G X (7 x 7 slices).  5 x 5 slices with pairs
+// s + t <= 6 saved 4 ms per config-1 solve but moved the largest bootstrap delta chi^2
+// against FP64 from 1.8e-3 to 1.5e-2 (the residual's error enters G^-1 directly).
+constexpr int kNsResidualLevels = 7;
 constexpr int kNsUpdateLevels = 5;     // slice pairs s + t <= 5 of the update X R (4 x 4 slices)
 
 constexpr int VS = 5;          // slices of the vector operands: 39 bits below each column's largest magnitude
@@ -737,7 +740,8 @@ static int mixed_setup(const smx_nnls_problem *p, const TL *lib, const int32_t *
         // (w = D + H^T (y - U D)), in place of U D, G^-1 E and U^T F.  U is overwritten
         // by H, and the slices of U^T (orbits over rows) by those of H^T.
         // pairs s + t <= 6: the pairs left out weigh 2^-40 of max|O| max|U| per term, far
-        // below the 31-bit slicing of U and of H itself
+        // below the 31-bit slicing of U and of H itself (4 slices of O with pairs
+        // s + t <= 5 moved the largest bootstrap delta chi^2 at config 1 to 0.16)
         split::Acc acc_h{Tacc, Racc, m};
         if ((st = split::gemm(sh.Xg, sh.Ut, acc_h, false, derr, s, 6))) return st;   // O U
         h_combine_kernel<<<grid1d(m * n), 256, 0, s>>>(Tacc, Racc, sh.Xg.expo, sh.Ut.expo, gdiag, U, m, n);
