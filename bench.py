@@ -1,16 +1,18 @@
 #!/usr/bin/env python
-"""Model evaluations per second on one GB300 (the config-1 workload).
+"""Model evaluations per second on one GB300.
 
-One step = one full model evaluation (model_likelihood): Jeans ICs ->
+Default (config 2, the batched workload): one step = one batch of 64 parameter
+points, each a full model evaluation (model_likelihood_batch): Jeans ICs ->
 16,384 particles x 4 jitter realisations integrated for 50 circular periods
 (adaptive BS23, rtol 1e-6, 1,000 uniform-time samples each) -> projection and
 binning into an 80x80-pixel / 400-aperture IFU and a 24x16x12 (R, z, phi)
 grid -> 3-D density target -> 100 bootstrap ADMM NNLS solves (200 iterations)
--> model maps -> chi^2 -> log-mean-exp.  Inputs are seeded synthetic data
-(schwarmax_gb300.synthetic); working sets are larger than L2 (the sample store
-alone is 1.8 GB), so no L2 flush is needed between steps.
+-> model maps -> chi^2 -> log-mean-exp.  --config 1, 4 or small: one evaluation
+of that configuration per step (model_likelihood).  Inputs are seeded synthetic
+data (schwarmax_gb300.synthetic); working sets are larger than L2 (the sample
+store of one evaluation alone is 1.8 GB), so no L2 flush is needed between steps.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--config 1|2|4|small]
 
 --impl reference times the CPU restatement of the same evaluation (oracle/,
 all host cores) on a bounded sample of the workload and scales it to evals/s.
@@ -29,9 +31,17 @@ sys.path.insert(0, ROOT)
 
 METRIC = "model evals/sec at Δχ²≤0.1, batched mixed-precision vs plain FP64, 1 GB300"
 UNIT = "evals/s"
-WORKLOAD = ("config1: 16,384 particles x 4 realisations, 50 circular periods, rtol 1e-6, 1,000 uniform-time "
-            "samples per orbit, 80x80 px / 400 Voronoi apertures, 24x16x12 Rzphi grid, 100 bootstrap ADMM "
-            "NNLS (200 iterations)")
+
+
+def workload(cfg):
+    """One evaluation of a configuration, in words."""
+    nR, nz, nphi = cfg.n_grid
+    return (f"{cfg.name}: {cfg.n_part:,} particles x {cfg.n_real} realisations, {cfg.n_periods:g} circular periods, "
+            f"rtol {cfg.rtol:g}, {cfg.n_samples:,} uniform-time samples per orbit, {cfg.n_pix}x{cfg.n_pix} px / "
+            f"{cfg.n_bins:,} Voronoi apertures, {nR}x{nz}x{nphi} Rzphi grid, {cfg.n_boot} bootstrap ADMM NNLS "
+            f"({cfg.admm_iters} iterations)")
+
+
 WORKLOAD_BATCH = ("config2: {P} parameter points per batch (potential within +-20% of config 1, Omega_p in "
                   "[25, 45] km/s/kpc), each 16,384 particles x 4 realisations, 50 circular periods, rtol 1e-6, "
                   "1,000 uniform-time samples per orbit, 80x80 px / 400 Voronoi apertures, 24x16x12 Rzphi grid, "
@@ -229,7 +239,7 @@ def run_ours(args, rank, world, local):
                 "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32 (orbits, binning) / bf16 split products + f64 (NNLS)",
                 "data": "synthetic (seeded; schwarmax_gb300.synthetic)",
-                "config": {"workload": WORKLOAD, "bootstrap": args.bootstrap, "parallelism": f"replicas x{world}",
+                "config": {"workload": workload(cfg), "bootstrap": args.bootstrap, "parallelism": f"replicas x{world}",
                            "l2": "working set > L2 (no flush)", "setup_s": round(setup_s, 1)},
                 "gpu_launches": int(launches), "roofline": roofline, "stages_ms": stages, "precision": prec, "e2e": e2e,
                 "cpu_baseline": cpu, "clocks": clocks, "logL_last": float(val.item())}
@@ -807,8 +817,9 @@ def run_reference(args, rank, world):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic (seeded)", "impl": "reference",
-            "config": {"workload": WORKLOAD}, "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores,
-                                                                 "kind": "port", "sample": sample},
+            "config": {"workload": workload(cfg) + ("; per parameter point of the 64-point batch (on the CPU a "
+                                                    "batch costs the sum of its points)" if args.config == 2 else "")},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
