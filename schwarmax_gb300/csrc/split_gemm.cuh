@@ -22,9 +22,10 @@
 //   the remaining levels share one FP32 accumulator.
 // Rows with one dominant element (the diagonal of an inverse) carry most of a
 // product in the lower levels, and the tensor cores' FP32 accumulation there
-// leaves a systematic error, so every slice pair is formed (LMAX = SA + SB)
-// with three exact levels (column tiles of 112 or 128) or five (64-wide
-// tiles); 7 x 7 products use four exact levels and pairs up to s + t = 8.
+// leaves a systematic error, so by default every slice pair is formed
+// (LMAX = SA + SB) with three exact levels (column tiles of 112 or 128) or five
+// (64-wide tiles); 7 x 7 products use four exact levels.  Callers whose operands
+// have no dominant element drop the pairs above a level (lmax below).
 // The result for output (i, j) is returned as the exact int64 T and a float R,
 // both accumulated with atomics over the k ranges of all CTAs, and the consumer
 // forms   C_ij = 2^(eA_i + eB_j - 14) (T_ij 2^-8(EXACT-1) + R_ij)   in double.
