@@ -725,8 +725,10 @@ def nnls_cpu_seconds(cfg, rng):
 def cpu_baseline(cfg, quick=True, cores=None):
     """The FP64 oracle on a bounded sample of the workload, scaled to evals/s.
 
-    Sample: n orbits of the config integrated over 1/25 of the horizon (2 of
-    50 periods) with the same tolerances, per-orbit cost scaled to
+    Sample: n orbits of the config (2,048, 10-20 s on one core; the oracle integrates
+    all orbits of a call as one vector, and its cost per orbit falls from 16 to 2,048
+    orbits by 28x as NumPy's per-step overhead is shared) integrated over 1/25 of the
+    horizon (2 of 50 periods) with the same tolerances, per-orbit cost scaled to
     n_part * n_real orbits and 50 periods; plus the oracle NNLS timed at a
     1/16-scale problem and scaled by its cost (nnls_cpu_seconds)."""
     import numpy as np
@@ -737,7 +739,7 @@ def cpu_baseline(cfg, quick=True, cores=None):
     halo, bary = unpack_params(theta)
     P = op.canonical_params(bary, halo, cfg.bulge_mass)
     rng = np.random.default_rng(3)
-    n = 16 if quick else 64
+    n = 2048 if quick else 8192
     pos = synthetic.disc_positions(rng, n)
     R = np.sqrt(pos[:, 0] ** 2 + pos[:, 1] ** 2)
     vc = oo.rotation_curve(R, pos[:, 2], P)
@@ -772,7 +774,9 @@ def _cpu_worker(args):
 
 
 def run_reference(args, rank, world):
-    """CPU restatement of the evaluation on all host cores (bounded sample)."""
+    """CPU restatement of the evaluation on all host cores (bounded sample: 512 orbits
+    per core, so that the oracle's vectorised integrator shares its per-step overhead
+    as the reference's vmapped one would)."""
     if rank != 0:
         return
     import multiprocessing as mp
@@ -787,7 +791,7 @@ def run_reference(args, rank, world):
     halo, bary = unpack_params(theta)
     P = op.canonical_params(bary, halo, cfg.bulge_mass)
     rng = np.random.default_rng(3)
-    per = 4
+    per = 512
     n = cores * per
     pos = synthetic.disc_positions(rng, n)
     R = np.sqrt(pos[:, 0] ** 2 + pos[:, 1] ** 2)
