@@ -185,6 +185,8 @@ _SIGS = {
     "smx_rmh_accept": ([_P, _P, _P, _P, _P, _P, ctypes.c_int, ctypes.c_int, _P, _P], ctypes.c_int),
     "smx_spd_inverse_f32_workspace_size": ([_I64, ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
     "smx_spd_inverse_f32": ([_P, _I64, _P, _P, ctypes.c_size_t, _P], ctypes.c_int),
+    "smx_spd_inverse_seed_workspace_size": ([_I64, ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
+    "smx_spd_inverse_seed": ([_P, _I64, _P, _P, ctypes.c_size_t, _P], ctypes.c_int),
     "smx_split_gemm_workspace_size": ([ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int, ctypes.c_int,
                                        ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
     "smx_split_gemm": ([ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P,

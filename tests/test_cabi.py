@@ -32,6 +32,8 @@ def test_library_exports_declared_symbols():
     for n in _declared():
         assert hasattr(lib, n), n
     assert set(_lib.EXPORTS) == set(_declared())
+    # every entry point has ctypes argument types (no default int conversion of 64-bit arguments)
+    assert set(_lib._SIGS) == set(_lib.EXPORTS)
     lib.smx_version.restype = ctypes.c_int
     assert lib.smx_version() >= 100
     lib.smx_status_string.restype = ctypes.c_char_p
@@ -123,6 +125,25 @@ def test_split_product_argument_errors_without_gpu():
     assert lib.smx_split_gemm(300, 100, 1000, 4, 5, 0, None, fake, fake, fake, need, None) == 1
     assert lib.smx_split_gemm(300, 200, 1000, 4, 4, 1, fake, fake, fake, fake, 1 << 40, None) == 1    # lower: M == N
     assert lib.smx_split_gemm(1 << 17, 1 << 15, 64, 4, 4, 0, fake, fake, fake, fake, 1 << 40, None) == 2  # too large
+
+
+def test_seed_inverse_argument_errors_without_gpu():
+    from schwarmax_gb300 import _lib
+    if not os.path.exists(_lib.LIB_PATH):
+        pytest.skip("library not built")
+    lib = _lib.load()
+    nbytes = ctypes.c_size_t(0)
+    assert lib.smx_spd_inverse_seed_workspace_size(6608, ctypes.byref(nbytes)) == 0
+    assert nbytes.value > 6608 * 6608 * (8 + 8 + 4)    # accumulators and the scratch block at least
+    assert lib.smx_spd_inverse_seed_workspace_size(12000, ctypes.byref(nbytes)) == 0
+    need = nbytes.value
+    assert need > 2 ** 32                               # passed as a size_t, not an int
+    assert lib.smx_spd_inverse_seed_workspace_size(0, ctypes.byref(nbytes)) == 1
+    assert lib.smx_spd_inverse_seed_workspace_size(100, None) == 1
+    fake = ctypes.c_void_p(256)
+    assert lib.smx_spd_inverse_seed(fake, 12000, fake, fake, need - 1, None) == 6   # workspace too small
+    assert lib.smx_spd_inverse_seed(None, 12000, fake, fake, need, None) == 1
+    assert lib.smx_spd_inverse_seed(fake, 0, fake, fake, need, None) == 1
 
 
 def test_nnls_argument_errors_without_gpu():
